@@ -1,0 +1,140 @@
+/*
+ * vnec_gb300 — GB300 (sm_103a) implementation of the OpenSparseBLAS VNEC mxv
+ * (sparse matrix x dense vector) path, behind the reference's own C API.
+ *
+ * Drop-in use: link libvnec_gb300.so in place of the reference's operation
+ * module; the reference's core objects (SpB_Matrix in CSR, dense SpB_Vector)
+ * are read in place.  Each entry point below names the reference declaration
+ * it replaces.  Functions with the _ext suffix are additions of this library.
+ *
+ * Semantics shared by all SpMV entry points: y := A x (overwrite, no
+ * accumulate), as in the reference kernels (spmv_vnec_L_for_mxv.c:145,
+ * spmv_vnec_D_for_mxv.c:452).  A handle is built once from A and uploads A to
+ * the GPU; the host-vector entry points copy x to the device and y back on
+ * every call.  Errors never exit the process: functions returning SpB_Info
+ * report SpB_FAILURE, void functions of the reference signature record the
+ * error, and SpB_VNEC_last_error_ext() returns the message of the calling
+ * thread's last failure.
+ */
+#ifndef VNEC_GB300_H
+#define VNEC_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifndef VNEC_HAVE_OPENSPARSEBLAS_H
+#include "vnec_spb_types.h"
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------------------ */
+/* Reference entry points                                                    */
+/* ------------------------------------------------------------------------ */
+
+/* include/OpenSparseBLAS.h:1951 (declared there, body commented out in
+ * src/operation/src/SpB_mxv.c:28-35).  y := A x.  VNEC is a handle returned by
+ * any Build_VNEC_* or SpB_VNEC_plan_ext of this library, or NULL: then a plan
+ * for A is built with the automatic selection and cached against A (the cache
+ * is keyed by A and its array pointers; call SpB_VNEC_forget_ext(A) after
+ * changing A in place). */
+SpB_Info SpB_mxv(SpB_Vector y, const SpB_Matrix A, const SpB_Vector x, void *VNEC);
+
+/* include/OpenSparseBLAS.h:1983 (ird_calc.c:2-122).  Returns SpB_VNEC_D when
+ * nnz / (blocks * nLanes) >= threshold, else SpB_VNEC_S, computed exactly as
+ * the reference's x86 build does (36 merge-path partitions, nLanes 8/16 and
+ * thresholds 0.477/0.437 for FP64/FP32, SpB_mxv.h:25-32).  Does not print. */
+SpB_VNEC_type IRD_VNEC(const SpB_Matrix A, SpB_Type type);
+
+/* include/OpenSparseBLAS.h:2023 (spmv_vnec_L_for_mxv.c:2-35).  Merge-path plan
+ * for A (FP64 or FP32 values).  The public fields num_merge_items and
+ * items_per_thread are filled; the pointer fields are NULL.  Release with
+ * VNEC_L_free_ext. */
+struct VNEC_L *Build_VNEC_L(const SpB_Matrix A);
+
+/* include/OpenSparseBLAS.h:2024 and :2073 (spmv_vnec_L_for_mxv.c:36-165). */
+void SpMV_VNEC_L_FP32(SpB_Vector y, const SpB_Matrix A, const SpB_Vector x, VNEC_L *mat_thd);
+void SpMV_VNEC_L_FP64(SpB_Vector y, const SpB_Matrix A, const SpB_Vector x, VNEC_L *mat_thd);
+
+/* ------------------------------------------------------------------------ */
+/* Handle release (the reference frees handles field by field in its test    */
+/* code, src/operation/test/test_spmv_vnec.hpp:81-176 and                     */
+/* test_spmv_vnec.cpp:248-253; these library functions replace that).        */
+/* ------------------------------------------------------------------------ */
+void VNEC_L_free_ext(VNEC_L *mat_thd);
+
+/* ------------------------------------------------------------------------ */
+/* Extensions                                                                */
+/* ------------------------------------------------------------------------ */
+
+/* Message of the calling thread's last failure ("" if none). */
+const char *SpB_VNEC_last_error_ext(void);
+
+/* Plan construction options (zero-initialise for defaults). */
+typedef enum {
+  SpB_VNEC_KERNEL_AUTO = 0,
+  SpB_VNEC_KERNEL_L = 1, /* merge-path CSR */
+  SpB_VNEC_KERNEL_D = 2, /* windowed dense blocks */
+  SpB_VNEC_KERNEL_S = 3  /* windowed sliced rows */
+} SpB_VNEC_kernel_ext;
+
+typedef struct {
+  int kernel;            /* SpB_VNEC_kernel_ext */
+  int threads_per_block; /* 0: default */
+  int items_per_thread;  /* 0: default */
+  int reserved[13];
+} SpB_VNEC_options_ext;
+
+/* Plan from raw host CSR arrays: int64 row offsets (n_rows + 1), int32
+ * columns and FP64/FP32 values (nnz = row_ptr[n_rows]).  The arrays are
+ * copied; the caller keeps ownership.  Returns NULL on failure. */
+void *SpB_VNEC_plan_ext(const SpB_VNEC_options_ext *opts, SpB_Type type, int64_t n_rows, int64_t n_cols,
+                        const int64_t *row_ptr, const int32_t *col, const void *val);
+
+/* Plan from a reference SpB_Matrix with explicit options. */
+void *SpB_VNEC_plan_matrix_ext(const SpB_VNEC_options_ext *opts, const SpB_Matrix A);
+
+/* Releases any plan or handle of this library (including Build_VNEC_*). */
+void SpB_VNEC_plan_free_ext(void *plan);
+
+/* Drops the plan SpB_mxv cached for A (no-op if none). */
+void SpB_VNEC_forget_ext(const SpB_Matrix A);
+
+/* y := A x with x and y in device memory, enqueued on `stream` (a
+ * cudaStream_t; NULL = legacy default stream) without synchronising.  Value
+ * type of x and y is the plan's (FP64 or FP32). */
+SpB_Info SpB_mxv_device_ext(void *plan, const void *d_x, void *d_y, void *stream);
+
+/* y := A x with host x and y (the SpB_mxv data path without SpB_Vector). */
+SpB_Info SpB_mxv_host_ext(void *plan, const void *h_x, void *h_y);
+
+/* Plan description. */
+typedef struct {
+  int kernel;              /* SpB_VNEC_kernel_ext actually built */
+  int value_type;          /* SpB_Type of x / y */
+  int64_t n_rows, n_cols, nnz;
+  int64_t device_bytes;    /* device memory held by the plan */
+  int64_t algorithmic_bytes; /* bytes one SpMV must move at minimum */
+  int launches_per_call;   /* kernels launched by one SpMV */
+  int threads_per_block;
+  int items_per_thread;
+  int64_t num_tiles;
+  int reserved[8];
+} SpB_VNEC_info_ext;
+
+SpB_Info SpB_VNEC_plan_info_ext(const void *plan, SpB_VNEC_info_ext *info);
+
+/* Per-kernel timing: when enabled, each SpMV of the plan records CUDA events
+ * around each of its kernels on the launching stream;
+ * SpB_VNEC_kernel_ms_ext waits for the last call and writes up to `cap`
+ * durations in milliseconds (the main kernel first).  Returns the count. */
+SpB_Info SpB_VNEC_set_profiling_ext(void *plan, int enable);
+int SpB_VNEC_kernel_ms_ext(const void *plan, float *ms, int cap);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* VNEC_GB300_H */

@@ -1,0 +1,172 @@
+"""ctypes bindings of the CPU oracle — TEST INFRASTRUCTURE ONLY.
+
+Only the tests, ``__graft_entry__.smoke()`` and the CPU-baseline legs of
+``bench.py`` may use this module, and only as the checker or the timed CPU
+baseline; the product library never calls it.
+
+* ``liboracle.so`` (``vnec_oracle.c``): the C restatement of the reference's
+  VNEC path, parameterised by partition count and lane width.
+* ``libvnec_ref.so`` (optional, built from the reference's own sources by
+  ``oracle/Makefile`` target ``ref``, x86 AVX-512 only): used to pin the
+  restatement and to generate the golden fixtures.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ORACLE_SO = os.path.join(HERE, "_build", "liboracle.so")
+REF_SO = os.path.join(HERE, "_ref", "libvnec_ref.so")
+
+# Compile-time constants of the reference builds (src/operation/include/SpB_mxv.h:17-32).
+X86 = dict(nparts=36, nlanes_f64=8, nlanes_f32=16, thr_f64=0.477, thr_f32=0.437)
+ARM = dict(nparts=48, nlanes_f64=2, nlanes_f32=4, thr_f64=0.76, thr_f32=0.543)
+
+_vp = C.c_void_p
+_i64 = C.c_int64
+_lib = None
+_ref = None
+
+
+def build() -> None:
+    """Builds liboracle.so (and the reference library when its sources exist here)."""
+    subprocess.run(["make", "-s", "-C", HERE], check=True)
+    if os.path.isdir("/root/reference/src/operation/src"):
+        subprocess.run(["make", "-s", "-C", HERE, "ref"], check=True)
+
+
+def lib() -> C.CDLL:
+    global _lib
+    if _lib is None:
+        if not os.path.exists(ORACLE_SO):
+            build()
+        L = C.CDLL(ORACLE_SO)
+        L.orc_spmv_serial_f64.argtypes = [_i64] + [_vp] * 5
+        L.orc_spmv_serial_f32.argtypes = [_i64] + [_vp] * 5
+        L.orc_spmv_neumaier_f64.argtypes = [_i64] + [_vp] * 6
+        L.orc_spmv_L_f64.argtypes = [C.c_int, _i64, _i64] + [_vp] * 5
+        L.orc_spmv_L_f32.argtypes = [C.c_int, C.c_int, _i64, _i64] + [_vp] * 5
+        for f in ("orc_spmv_D_f64", "orc_spmv_S_f64", "orc_spmv_D_f32", "orc_spmv_S_f32"):
+            getattr(L, f).argtypes = [C.c_int, C.c_int, _i64, _i64, _i64] + [_vp] * 5 + [C.c_int]
+        L.orc_ird.argtypes = [C.c_int, C.c_int, C.c_float, _i64, _i64, _i64, _vp, _vp, _vp]
+        L.orc_ird.restype = C.c_int
+        L.orc_partition.argtypes = [C.c_int, _i64, _i64, _vp, _vp, _vp, _vp, _vp]
+        L.orc_time_L_f64.argtypes = [C.c_int, _i64, _i64] + [_vp] * 5 + [C.c_int, C.c_int]
+        L.orc_time_L_f64.restype = C.c_double
+        L.orc_num_procs.restype = C.c_int
+        _lib = L
+    return _lib
+
+
+def ref_available() -> bool:
+    return os.path.exists(REF_SO)
+
+
+def ref() -> C.CDLL:
+    global _ref
+    if _ref is None:
+        R = C.CDLL(REF_SO)
+        for f in ("ref_spmv_f64", "ref_spmv_f32"):
+            getattr(R, f).argtypes = [C.c_int, _i64, _i64, _i64] + [_vp] * 6
+            getattr(R, f).restype = C.c_int
+        R.ref_ird.argtypes = [C.c_int, _i64, _i64, _i64, _vp, _vp, _vp, _vp]
+        R.ref_ird.restype = C.c_int
+        R.ref_time_L_f64.argtypes = [_i64, _i64, _i64] + [_vp] * 4 + [C.c_int, C.c_int]
+        R.ref_time_L_f64.restype = C.c_double
+        _ref = R
+    return _ref
+
+
+def _p(a: np.ndarray) -> int:
+    return a.ctypes.data
+
+
+def _csr(m):
+    rp = np.ascontiguousarray(m.row_ptr, dtype=np.int64)
+    ci = np.ascontiguousarray(m.col, dtype=np.int32)
+    return rp, ci
+
+
+def spmv_serial(m, x, dtype=np.float64) -> np.ndarray:
+    """SpB_mxv_FP64_serial / _FP32_serial (test_spmv_vnec.hpp:34-79)."""
+    rp, ci = _csr(m)
+    v = np.ascontiguousarray(m.val, dtype=dtype)
+    xx = np.ascontiguousarray(x, dtype=dtype)
+    y = np.zeros(m.n_rows, dtype=dtype)
+    f = lib().orc_spmv_serial_f64 if dtype == np.float64 else lib().orc_spmv_serial_f32
+    f(m.n_rows, _p(rp), _p(ci), _p(v), _p(xx), _p(y))
+    return y
+
+
+def spmv_neumaier(m, x) -> tuple[np.ndarray, np.ndarray]:
+    """Compensated FP64 SpMV and the row conditioning sum_j |a_ij x_j|."""
+    rp, ci = _csr(m)
+    v = np.ascontiguousarray(m.val, dtype=np.float64)
+    xx = np.ascontiguousarray(x, dtype=np.float64)
+    y = np.zeros(m.n_rows)
+    cond = np.zeros(m.n_rows)
+    lib().orc_spmv_neumaier_f64(m.n_rows, _p(rp), _p(ci), _p(v), _p(xx), _p(y), _p(cond))
+    return y, cond
+
+
+def spmv_vnec(variant: str, m, x, dtype=np.float64, build=X86) -> np.ndarray:
+    """The restated reference kernels: variant in {'L', 'D', 'S'}."""
+    rp, ci = _csr(m)
+    v = np.ascontiguousarray(m.val, dtype=dtype)
+    xx = np.ascontiguousarray(x, dtype=dtype)
+    y = np.zeros(m.n_rows, dtype=dtype)
+    L = lib()
+    f64 = dtype == np.float64
+    nl = build["nlanes_f64"] if f64 else build["nlanes_f32"]
+    if variant == "L":
+        if f64:
+            L.orc_spmv_L_f64(build["nparts"], m.n_rows, m.nnz, _p(rp), _p(ci), _p(v), _p(xx), _p(y))
+        else:
+            L.orc_spmv_L_f32(build["nparts"], nl, m.n_rows, m.nnz, _p(rp), _p(ci), _p(v), _p(xx), _p(y))
+    else:
+        f = getattr(L, f"orc_spmv_{variant}_{'f64' if f64 else 'f32'}")
+        f(build["nparts"], nl, m.n_rows, m.n_cols, m.nnz, _p(rp), _p(ci), _p(v), _p(xx), _p(y), 1)
+    return y
+
+
+def ird(m, fp64: bool = True, build=X86) -> tuple[int, float]:
+    """IRD_VNEC restated: (SpB_VNEC_D=0 / SpB_VNEC_S=1, ratio)."""
+    rp, ci = _csr(m)
+    out = np.zeros(1, dtype=np.float32)
+    nl = build["nlanes_f64"] if fp64 else build["nlanes_f32"]
+    thr = build["thr_f64"] if fp64 else build["thr_f32"]
+    t = lib().orc_ird(build["nparts"], nl, C.c_float(thr), m.n_rows, m.n_cols, m.nnz, _p(rp), _p(ci), _p(out))
+    return t, float(out[0])
+
+
+def time_L_f64(m, x, nparts: int, warm: int = 1, reps: int = 40) -> float:
+    """Seconds per SpMV_VNEC_L_FP64 call of the restatement (OpenMP, nparts threads)."""
+    rp, ci = _csr(m)
+    v = np.ascontiguousarray(m.val, dtype=np.float64)
+    xx = np.ascontiguousarray(x, dtype=np.float64)
+    y = np.zeros(m.n_rows)
+    return lib().orc_time_L_f64(nparts, m.n_rows, m.nnz, _p(rp), _p(ci), _p(v), _p(xx), _p(y), warm, reps)
+
+
+def ref_spmv(variant: int, m, x, dtype=np.float64) -> tuple[np.ndarray, int, float]:
+    """The reference build itself: variant 0 auto (harness dispatch), 1 D, 2 S, 3 L, 4 serial."""
+    rp, ci = _csr(m)
+    v = np.ascontiguousarray(m.val, dtype=dtype)
+    xx = np.ascontiguousarray(x, dtype=dtype)
+    y = np.zeros(m.n_rows, dtype=dtype)
+    irdv = np.zeros(1, dtype=np.float32)
+    f = ref().ref_spmv_f64 if dtype == np.float64 else ref().ref_spmv_f32
+    used = f(variant, m.n_rows, m.n_cols, m.nnz, _p(rp), _p(ci), _p(v), _p(xx), _p(y), _p(irdv))
+    return y, used, float(irdv[0])
+
+
+def rowwise_error(y: np.ndarray, y_ref: np.ndarray, cond: np.ndarray) -> np.ndarray:
+    """|y_i - yref_i| / sum_j |a_ij x_j| (0 where the row's conditioning sum is 0)."""
+    d = np.abs(y.astype(np.float64) - y_ref)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        e = np.where(cond > 0, d / np.where(cond > 0, cond, 1.0), d)
+    return e

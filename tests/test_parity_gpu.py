@@ -1,0 +1,203 @@
+"""GPU parity of the merge-path (VNEC-L counterpart) kernels, through the C ABI.
+
+Criteria (row-wise, conditioning-aware, against the compensated FP64 oracle):
+  FP64:  |y_i - yhat_i| <= 1e-12 * sum_j |a_ij x_j|
+  FP32:  |y_i - yhat_i| <= 1e-4  * sum_j |a_ij x_j|   (the reference's FP32
+         test bound is 1e-4 relative, test_spmv_vnec.cpp:132)
+Known-answer inputs (A_ij = i, x_j = j) must match bit for bit.
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from conftest import golden_cases, golden_csr, load_golden
+
+pytestmark = pytest.mark.gpu
+
+TOL_F64 = 1e-12
+TOL_F32 = 1e-4
+
+
+def check_f64(y, m, x, tol=TOL_F64):
+    from oracle import oracle as O
+
+    y_ref, cond = O.spmv_neumaier(m, x)
+    err = np.abs(y - y_ref)
+    bad = err > tol * cond
+    assert not bad.any(), f"{bad.sum()} rows exceed {tol}*cond; worst {np.max(err / np.maximum(cond, 1e-300))}"
+
+
+def check_f32(y, m, x, tol=TOL_F32):
+    from oracle import oracle as O
+
+    m64 = type(m)(m.n_rows, m.n_cols, m.row_ptr, m.col, np.asarray(m.val, dtype=np.float32).astype(np.float64))
+    y_ref, cond = O.spmv_neumaier(m64, np.asarray(x, dtype=np.float32).astype(np.float64))
+    err = np.abs(y.astype(np.float64) - y_ref)
+    assert np.all(err <= tol * cond + 1e-30)
+
+
+@pytest.mark.parametrize("case", golden_cases())
+def test_golden_fp64_dropin(built, case):
+    """Build_VNEC_L + SpMV_VNEC_L_FP64 on reference-layout objects vs the
+    reference's own outputs."""
+    from vnec_gb300 import api
+
+    g = load_golden(case)
+    m = golden_csr(g)
+    A = api.Matrix.from_csr(m)
+    x = api.Vector(g["x"])
+    y = api.Vector(n=m.n_rows)
+    h = api.Build_VNEC_L(A)
+    try:
+        api.SpMV_VNEC_L_FP64(y, A, x, h)
+    finally:
+        api.VNEC_L_free(h)
+    if case.startswith("kat_"):
+        assert y.values.tobytes() == g["y_serial_f64"].tobytes()
+    else:
+        check_f64(y.values, m, g["x"])
+        _, cond = __import__("oracle.oracle", fromlist=["x"]).spmv_neumaier(m, g["x"])
+        for key in ("y_serial_f64", "y_L_f64"):
+            assert np.all(np.abs(y.values - g[key]) <= 2 * TOL_F64 * cond + 1e-300), key
+
+
+@pytest.mark.parametrize("case", golden_cases())
+def test_golden_fp32_dropin(built, case):
+    from vnec_gb300 import api
+
+    g = load_golden(case)
+    m = golden_csr(g)
+    A = api.Matrix.from_csr(m, dtype=np.float32)
+    x = api.Vector(g["x"], dtype=np.float32)
+    y = api.Vector(n=m.n_rows, dtype=np.float32)
+    h = api.Build_VNEC_L(A)
+    try:
+        api.SpMV_VNEC_L_FP32(y, A, x, h)
+    finally:
+        api.VNEC_L_free(h)
+    check_f32(y.values, m, g["x"])
+
+
+def test_spb_mxv_auto_plan_and_cache(built):
+    from vnec_gb300 import api
+    from vnec_gb300 import generators as G
+
+    m = G.lognormal(30000, seed=3)
+    xv = G.vector(m.n_cols, seed=4)
+    A = api.Matrix.from_csr(m)
+    x, y = api.Vector(xv), api.Vector(n=m.n_rows)
+    api.SpB_mxv(y, A, x)
+    first = y.values.copy()
+    check_f64(first, m, xv)
+    y.values[:] = 0
+    api.SpB_mxv(y, A, x)  # cached plan
+    assert y.values.tobytes() == first.tobytes()  # deterministic
+    api.lib().SpB_VNEC_forget_ext(A.handle)
+
+
+@pytest.mark.parametrize("tpb,ipt", [(128, 4), (128, 7), (128, 10), (256, 4), (256, 7), (256, 10)])
+def test_tile_shapes(built, tpb, ipt):
+    from vnec_gb300 import api
+    from vnec_gb300 import generators as G
+
+    for m in (G.rmat(16, 16 << 16, seed=7), G.lognormal(20000, sigma=2.5, cap=4096, seed=8)):
+        xv = G.vector(m.n_cols, seed=9)
+        p = api.Plan(m, kernel=api.KERNEL_L, threads_per_block=tpb, items_per_thread=ipt)
+        y = p.mxv_host(xv)
+        check_f64(y, m, xv)
+        assert p.info().num_tiles == -(-(m.n_rows + m.nnz) // (tpb * ipt))
+        p.free()
+
+
+def _custom(n_rows, n_cols, lens, seed=0):
+    from vnec_gb300 import generators as G
+
+    rng = np.random.default_rng(seed)
+    row_ptr = np.zeros(n_rows + 1, dtype=np.int64)
+    row_ptr[1:] = np.cumsum(lens)
+    cols = [np.sort(rng.choice(n_cols, size=int(k), replace=False)) for k in lens]
+    col = np.concatenate(cols).astype(np.int32) if len(cols) else np.zeros(0, np.int32)
+    return G.from_arrays(n_rows, n_cols, row_ptr, col, rng.uniform(-1, 1, size=int(row_ptr[-1])))
+
+
+@pytest.mark.parametrize("name", ["empty_matrix", "single_row_spanning_tiles", "all_rows_empty",
+                                  "single_entry", "rectangular_wide", "rectangular_tall", "tile_boundary",
+                                  "hub_rows_and_empties"])
+def test_edge_cases(built, name):
+    from vnec_gb300 import api
+
+    if name == "empty_matrix":
+        m = _custom(37, 41, np.zeros(37, dtype=int))
+    elif name == "single_row_spanning_tiles":
+        m = _custom(1, 200000, [150000])
+    elif name == "all_rows_empty":
+        m = _custom(5000, 5000, np.zeros(5000, dtype=int))
+    elif name == "single_entry":
+        m = _custom(1, 1, [1])
+    elif name == "rectangular_wide":
+        m = _custom(100, 1_000_000, np.full(100, 300))
+    elif name == "rectangular_tall":
+        m = _custom(200000, 10, np.random.default_rng(1).integers(0, 11, size=200000))
+    elif name == "tile_boundary":
+        # n_rows + nnz = 3 * 1792 exactly (default tile of 256 x 7 items), then +-1
+        m = _custom(896, 896, np.full(896, 5))
+    else:
+        rng = np.random.default_rng(5)
+        lens = np.where(rng.random(4000) < 0.5, 0, rng.integers(1, 20, size=4000))
+        lens[[10, 2000, 3999]] = [30000, 45000, 29000]
+        m = _custom(4000, 60000, lens, seed=6)
+    xv = np.random.default_rng(2).uniform(-1, 1, size=m.n_cols)
+    for tpb, ipt in ((256, 7), (128, 4)):
+        p = api.Plan(m, kernel=api.KERNEL_L, threads_per_block=tpb, items_per_thread=ipt)
+        y = p.mxv_host(xv)
+        check_f64(y, m, xv)
+        p.free()
+
+
+def test_device_pointers_on_torch_stream(built):
+    import torch
+
+    from vnec_gb300 import api
+    from vnec_gb300 import generators as G
+
+    m = G.rmat(15, 16 << 15, seed=11)
+    xv = G.vector(m.n_cols, seed=12)
+    p = api.Plan(m, kernel=api.KERNEL_L)
+    x = torch.from_numpy(xv).cuda()
+    y = torch.full((m.n_rows,), float("nan"), dtype=torch.float64, device="cuda")
+    s = torch.cuda.Stream()
+    with torch.cuda.stream(s):
+        p.mxv_device(x.data_ptr(), y.data_ptr(), s.cuda_stream)
+    s.synchronize()
+    check_f64(y.cpu().numpy(), m, xv)
+    p.set_profiling(True)
+    with torch.cuda.stream(s):
+        p.mxv_device(x.data_ptr(), y.data_ptr(), s.cuda_stream)
+    ms = p.kernel_ms()
+    assert len(ms) == 2 and all(t > 0 for t in ms)
+    p.free()
+
+
+def test_full_size_rmat_scale24(built):
+    """The benchmark matrix itself (2^24 rows, 2^28 generated edges): tolerance
+    against the oracle and the known-answer pattern on the same structure."""
+    from vnec_gb300 import api
+    from vnec_gb300 import generators as G
+
+    m = G.rmat(24, 1 << 28, seed=1)
+    xv = G.vector(m.n_cols, seed=2)
+    p = api.Plan(m, kernel=api.KERNEL_L)
+    y = p.mxv_host(xv)
+    check_f64(y, m, xv)
+    y2 = p.mxv_host(xv)
+    assert y.tobytes() == y2.tobytes()
+    p.free()
+    kat, xk = G.kat_values(m)
+    rows = np.repeat(np.arange(m.n_rows, dtype=np.float64), np.diff(m.row_ptr))
+    exact = np.arange(m.n_rows, dtype=np.float64) * np.bincount(
+        rows.astype(np.int64), weights=m.col[: m.nnz].astype(np.float64), minlength=m.n_rows)
+    assert exact.max() < 2.0 ** 53
+    pk = api.Plan(kat, kernel=api.KERNEL_L)
+    assert pk.mxv_host(xk).tobytes() == exact.tobytes()
+    pk.free()

@@ -1,0 +1,280 @@
+"""Python mirror of the OpenSparseBLAS VNEC mxv interface, over the C ABI.
+
+The functions keep the reference's names and argument meaning
+(``include/OpenSparseBLAS.h:1951-2073``): ``IRD_VNEC``, ``Build_VNEC_L``,
+``SpMV_VNEC_L_FP64``, ``SpB_mxv`` ... operate on :class:`Matrix` and
+:class:`Vector`, which own reference-layout objects (``SpB_Matrix_CSC_or_CSR``
+with 64-bit ``SpB_Index`` offsets and columns, ``SpB_Vector_Dense``), so the
+calls exercise exactly the entry points a C caller of the reference would.
+Errors raise :class:`VnecError` carrying the library's last-error message —
+the reference exits the process instead (``src/core/src/SpB_Error.c:4-8``).
+
+Everything runs through ``libvnec_gb300.so``; nothing here computes on the CPU.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _loader
+
+# Enum values of include/vnec_spb_types.h (mirroring include/OpenSparseBLAS.h).
+SpB_SUCCESS, SpB_FAILURE = 0, 1
+SpB_FP32, SpB_FP64 = 10, 11
+SpB_DENSE = 0
+SpB_CSC, SpB_CSR = 0, 1
+SpB_VNEC_D, SpB_VNEC_S = 0, 1
+KERNEL_AUTO, KERNEL_L, KERNEL_D, KERNEL_S = 0, 1, 2, 3
+
+_DTYPE = {SpB_FP32: np.float32, SpB_FP64: np.float64}
+
+
+class VnecError(RuntimeError):
+    """A C-ABI call reported failure; the message is the library's last error."""
+
+
+class _MatrixBase(C.Structure):
+    _fields_ = [("element_type", C.c_int), ("format_type", C.c_int), ("row", C.c_uint64),
+                ("col", C.c_uint64), ("element_size", C.c_size_t)]
+
+
+class _CsrStruct(C.Structure):
+    _fields_ = [("matrix_base", _MatrixBase), ("val", C.c_void_p), ("indices", C.POINTER(C.c_uint64)),
+                ("ptr", C.POINTER(C.c_uint64)), ("ptr_len", C.c_uint64), ("nnz", C.c_uint64),
+                ("capacity", C.c_uint64)]
+
+
+class _VectorBase(C.Structure):
+    _fields_ = [("element_type", C.c_int), ("format_type", C.c_int), ("n", C.c_uint64),
+                ("element_size", C.c_size_t)]
+
+
+class _DenseStruct(C.Structure):
+    _fields_ = [("vector_base", _VectorBase), ("values", C.c_void_p)]
+
+
+class Options(C.Structure):
+    """SpB_VNEC_options_ext."""
+
+    _fields_ = [("kernel", C.c_int), ("threads_per_block", C.c_int), ("items_per_thread", C.c_int),
+                ("reserved", C.c_int * 13)]
+
+
+class Info(C.Structure):
+    """SpB_VNEC_info_ext."""
+
+    _fields_ = [("kernel", C.c_int), ("value_type", C.c_int), ("n_rows", C.c_int64), ("n_cols", C.c_int64),
+                ("nnz", C.c_int64), ("device_bytes", C.c_int64), ("algorithmic_bytes", C.c_int64),
+                ("launches_per_call", C.c_int), ("threads_per_block", C.c_int), ("items_per_thread", C.c_int),
+                ("num_tiles", C.c_int64), ("reserved", C.c_int * 8)]
+
+
+_vp = C.c_void_p
+
+
+def lib() -> C.CDLL:
+    """The loaded C-ABI library, with argument types declared."""
+    L = _loader.load("vnec_gb300")
+    if getattr(L, "_vnec_typed", False):
+        return L
+    L.SpB_mxv.argtypes = [_vp, _vp, _vp, _vp]
+    L.SpB_mxv.restype = C.c_int
+    L.IRD_VNEC.argtypes = [_vp, C.c_int]
+    L.IRD_VNEC.restype = C.c_int
+    L.Build_VNEC_L.argtypes = [_vp]
+    L.Build_VNEC_L.restype = _vp
+    for f in ("SpMV_VNEC_L_FP64", "SpMV_VNEC_L_FP32"):
+        getattr(L, f).argtypes = [_vp, _vp, _vp, _vp]
+        getattr(L, f).restype = None
+    L.VNEC_L_free_ext.argtypes = [_vp]
+    L.VNEC_L_free_ext.restype = None
+    L.SpB_VNEC_last_error_ext.argtypes = []
+    L.SpB_VNEC_last_error_ext.restype = C.c_char_p
+    L.SpB_VNEC_plan_ext.argtypes = [C.POINTER(Options), C.c_int, C.c_int64, C.c_int64, _vp, _vp, _vp]
+    L.SpB_VNEC_plan_ext.restype = _vp
+    L.SpB_VNEC_plan_matrix_ext.argtypes = [C.POINTER(Options), _vp]
+    L.SpB_VNEC_plan_matrix_ext.restype = _vp
+    L.SpB_VNEC_plan_free_ext.argtypes = [_vp]
+    L.SpB_VNEC_plan_free_ext.restype = None
+    L.SpB_VNEC_forget_ext.argtypes = [_vp]
+    L.SpB_VNEC_forget_ext.restype = None
+    L.SpB_mxv_device_ext.argtypes = [_vp, _vp, _vp, _vp]
+    L.SpB_mxv_device_ext.restype = C.c_int
+    L.SpB_mxv_host_ext.argtypes = [_vp, _vp, _vp]
+    L.SpB_mxv_host_ext.restype = C.c_int
+    L.SpB_VNEC_plan_info_ext.argtypes = [_vp, C.POINTER(Info)]
+    L.SpB_VNEC_plan_info_ext.restype = C.c_int
+    L.SpB_VNEC_set_profiling_ext.argtypes = [_vp, C.c_int]
+    L.SpB_VNEC_set_profiling_ext.restype = C.c_int
+    L.SpB_VNEC_kernel_ms_ext.argtypes = [_vp, C.POINTER(C.c_float), C.c_int]
+    L.SpB_VNEC_kernel_ms_ext.restype = C.c_int
+    L._vnec_typed = True
+    return L
+
+
+def last_error() -> str:
+    return lib().SpB_VNEC_last_error_ext().decode()
+
+
+def _check(ok: bool, what: str) -> None:
+    if not ok:
+        raise VnecError(f"{what}: {last_error()}")
+
+
+class Matrix:
+    """A CSR matrix in the reference's object layout (64-bit offsets/columns)."""
+
+    def __init__(self, n_rows: int, n_cols: int, row_ptr, col, val, dtype=np.float64):
+        self.ptr = np.ascontiguousarray(row_ptr, dtype=np.uint64)
+        self.indices = np.ascontiguousarray(col, dtype=np.uint64)
+        self.val = np.ascontiguousarray(val, dtype=dtype)
+        if self.ptr.shape != (n_rows + 1,):
+            raise ValueError("row_ptr must have n_rows + 1 entries")
+        nnz = int(self.ptr[-1]) if n_rows >= 0 else 0
+        self.type = SpB_FP64 if self.val.dtype == np.float64 else SpB_FP32
+        s = _CsrStruct()
+        s.matrix_base.element_type = self.type
+        s.matrix_base.format_type = SpB_CSR
+        s.matrix_base.row = n_rows
+        s.matrix_base.col = n_cols
+        s.matrix_base.element_size = self.val.itemsize
+        s.val = self.val.ctypes.data
+        s.indices = self.indices.ctypes.data_as(C.POINTER(C.c_uint64))
+        s.ptr = self.ptr.ctypes.data_as(C.POINTER(C.c_uint64))
+        s.ptr_len = n_rows + 1
+        s.nnz = nnz
+        s.capacity = nnz
+        self._s = s
+        self.n_rows, self.n_cols, self.nnz = n_rows, n_cols, nnz
+
+    @classmethod
+    def from_csr(cls, m, dtype=np.float64) -> "Matrix":
+        """From any object with n_rows, n_cols, row_ptr, col, val (e.g. generators.HostCSR)."""
+        return cls(m.n_rows, m.n_cols, m.row_ptr, m.col, np.asarray(m.val).astype(dtype, copy=False), dtype=dtype)
+
+    @property
+    def handle(self) -> int:
+        return C.addressof(self._s)
+
+
+class Vector:
+    """A dense vector in the reference's object layout (host values)."""
+
+    def __init__(self, values=None, n: int | None = None, dtype=np.float64, pinned_buffer=None):
+        if pinned_buffer is not None:
+            self.values = pinned_buffer
+        elif values is not None:
+            self.values = np.ascontiguousarray(values, dtype=dtype)
+        else:
+            self.values = np.zeros(n, dtype=dtype)
+        self.type = SpB_FP64 if self.values.dtype == np.float64 else SpB_FP32
+        s = _DenseStruct()
+        s.vector_base.element_type = self.type
+        s.vector_base.format_type = SpB_DENSE
+        s.vector_base.n = self.values.shape[0]
+        s.vector_base.element_size = self.values.itemsize
+        s.values = self.values.ctypes.data
+        self._s = s
+
+    @property
+    def handle(self) -> int:
+        return C.addressof(self._s)
+
+
+# --- reference entry points -------------------------------------------------
+
+def IRD_VNEC(A: Matrix, type_: int = SpB_FP64) -> int:
+    r = lib().IRD_VNEC(A.handle, type_)
+    _check(last_error() == "", "IRD_VNEC")
+    return r
+
+
+def Build_VNEC_L(A: Matrix) -> int:
+    h = lib().Build_VNEC_L(A.handle)
+    _check(bool(h), "Build_VNEC_L")
+    return h
+
+
+def SpMV_VNEC_L_FP64(y: Vector, A: Matrix, x: Vector, h: int) -> None:
+    lib().SpMV_VNEC_L_FP64(y.handle, A.handle, x.handle, h)
+    _check(last_error() == "", "SpMV_VNEC_L_FP64")
+
+
+def SpMV_VNEC_L_FP32(y: Vector, A: Matrix, x: Vector, h: int) -> None:
+    lib().SpMV_VNEC_L_FP32(y.handle, A.handle, x.handle, h)
+    _check(last_error() == "", "SpMV_VNEC_L_FP32")
+
+
+def VNEC_L_free(h: int) -> None:
+    lib().VNEC_L_free_ext(h)
+
+
+def SpB_mxv(y: Vector, A: Matrix, x: Vector, vnec: int | None = None) -> None:
+    _check(lib().SpB_mxv(y.handle, A.handle, x.handle, vnec) == SpB_SUCCESS, "SpB_mxv")
+
+
+# --- extensions ---------------------------------------------------------------
+
+def options(kernel: int = KERNEL_AUTO, threads_per_block: int = 0, items_per_thread: int = 0) -> Options:
+    o = Options()
+    o.kernel, o.threads_per_block, o.items_per_thread = kernel, threads_per_block, items_per_thread
+    return o
+
+
+class Plan:
+    """An owned plan (any kernel) built from raw CSR arrays or a Matrix."""
+
+    def __init__(self, csr=None, *, matrix: Matrix | None = None, dtype=np.float64, opts: Options | None = None,
+                 **kw):
+        o = opts or options(**kw)
+        L = lib()
+        if matrix is not None:
+            h = L.SpB_VNEC_plan_matrix_ext(C.byref(o), matrix.handle)
+            self.type = matrix.type
+        else:
+            rp = np.ascontiguousarray(csr.row_ptr, dtype=np.int64)
+            ci = np.ascontiguousarray(csr.col, dtype=np.int32)
+            vv = np.ascontiguousarray(csr.val, dtype=dtype)
+            self.type = SpB_FP64 if vv.dtype == np.float64 else SpB_FP32
+            h = L.SpB_VNEC_plan_ext(C.byref(o), self.type, csr.n_rows, csr.n_cols, rp.ctypes.data,
+                                    ci.ctypes.data, vv.ctypes.data)
+        _check(bool(h), "plan")
+        self.h = h
+        self.dtype = _DTYPE[self.type]
+
+    def info(self) -> Info:
+        inf = Info()
+        _check(lib().SpB_VNEC_plan_info_ext(self.h, C.byref(inf)) == SpB_SUCCESS, "plan_info")
+        return inf
+
+    def mxv_device(self, d_x: int, d_y: int, stream: int = 0) -> None:
+        """y = A x for device pointers (e.g. torch tensor data_ptr()) on a CUDA stream."""
+        _check(lib().SpB_mxv_device_ext(self.h, d_x, d_y, stream or None) == SpB_SUCCESS, "SpB_mxv_device_ext")
+
+    def mxv_host(self, x: np.ndarray, y: np.ndarray | None = None) -> np.ndarray:
+        inf_rows = self.info().n_rows
+        x = np.ascontiguousarray(x, dtype=self.dtype)
+        if y is None:
+            y = np.empty(inf_rows, dtype=self.dtype)
+        _check(lib().SpB_mxv_host_ext(self.h, x.ctypes.data, y.ctypes.data) == SpB_SUCCESS, "SpB_mxv_host_ext")
+        return y
+
+    def set_profiling(self, on: bool = True) -> None:
+        _check(lib().SpB_VNEC_set_profiling_ext(self.h, int(on)) == SpB_SUCCESS, "set_profiling")
+
+    def kernel_ms(self) -> list[float]:
+        buf = (C.c_float * 8)()
+        n = lib().SpB_VNEC_kernel_ms_ext(self.h, buf, 8)
+        return [buf[i] for i in range(n)]
+
+    def free(self) -> None:
+        if self.h:
+            lib().SpB_VNEC_plan_free_ext(self.h)
+            self.h = None
+
+    def __del__(self):  # pragma: no cover
+        try:
+            self.free()
+        except Exception:
+            pass

@@ -1,0 +1,288 @@
+// Exported C ABI: the reference's VNEC entry points and this library's
+// extensions (declarations and reference citations in include/vnec_gb300.h).
+
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+#include <unordered_map>
+
+#include "host.h"
+
+using namespace vnec;
+
+namespace {
+
+// Public VNEC_L handles are calloc'd blocks registered against their plan.
+// Putting nothing but the public struct in the block keeps the reference
+// harness's field-by-field cleanup (free of NULL fields, then free(handle))
+// memory-safe.
+template <typename Pub>
+Pub* publish(std::unique_ptr<Plan> plan) {
+  if (!plan) return nullptr;
+  auto* pub = static_cast<Pub*>(std::calloc(1, sizeof(Pub)));
+  if (!pub) {
+    set_error("out of host memory");
+    return nullptr;
+  }
+  register_plan(pub, std::move(plan));
+  return pub;
+}
+
+bool host_vector(const SpB_Vector v, SpB_Type type, int64_t n, void** values) {
+  if (!v) {
+    set_error("vector is NULL");
+    return false;
+  }
+  if (v->format_type != SpB_DENSE) {
+    set_error("vector must be dense (SpB_DENSE)");
+    return false;
+  }
+  if (v->element_type != type) {
+    set_error("vector element type does not match the matrix");
+    return false;
+  }
+  if ((int64_t)v->n != n) {
+    set_error("vector length does not match the matrix");
+    return false;
+  }
+  *values = reinterpret_cast<const SpB_Vector_Dense*>(v)->values;
+  if (n > 0 && !*values) {
+    set_error("vector storage is NULL");
+    return false;
+  }
+  return true;
+}
+
+// Plans cached by SpB_mxv(..., NULL): keyed by the matrix object, validated
+// against its array pointers and sizes.
+struct CacheKey {
+  const void* ptr;
+  const void* idx;
+  const void* val;
+  int64_t nnz, rows, cols;
+};
+std::mutex g_cache_mu;
+std::unordered_map<const void*, std::pair<CacheKey, std::unique_ptr<Plan>>>& auto_cache() {
+  static auto* c = new std::unordered_map<const void*, std::pair<CacheKey, std::unique_ptr<Plan>>>();
+  return *c;
+}
+
+CacheKey key_of(const SpB_Matrix A) {
+  auto* m = reinterpret_cast<const SpB_Matrix_CSC_or_CSR*>(A);
+  return CacheKey{m->ptr, m->indices, m->val, (int64_t)m->nnz, (int64_t)A->row, (int64_t)A->col};
+}
+
+bool same_key(const CacheKey& a, const CacheKey& b) {
+  return a.ptr == b.ptr && a.idx == b.idx && a.val == b.val && a.nnz == b.nnz && a.rows == b.rows && a.cols == b.cols;
+}
+
+std::unique_ptr<Plan> build_from_view(const CsrView& v, const SpB_VNEC_options_ext* opts) {
+  int kernel = opts ? opts->kernel : SpB_VNEC_KERNEL_AUTO;
+  switch (kernel) {
+    case SpB_VNEC_KERNEL_AUTO:
+    case SpB_VNEC_KERNEL_L:
+      return build_merge_path(v, opts);
+    default:
+      set_error("requested kernel is not available");
+      return nullptr;
+  }
+}
+
+Plan* plan_for_mxv(const SpB_Matrix A, void* handle) {
+  if (handle) {
+    Plan* p = find_plan(handle);
+    if (!p) set_error("unknown VNEC handle (not created by this library or already freed)");
+    return p;
+  }
+  CacheKey k = key_of(A);
+  {
+    std::lock_guard<std::mutex> g(g_cache_mu);
+    auto it = auto_cache().find(A);
+    if (it != auto_cache().end() && same_key(it->second.first, k)) return it->second.second.get();
+  }
+  CsrView v;
+  if (!view_from_matrix(A, &v)) return nullptr;
+  std::unique_ptr<Plan> p = build_from_view(v, nullptr);
+  if (!p) return nullptr;
+  Plan* raw = p.get();
+  std::lock_guard<std::mutex> g(g_cache_mu);
+  auto_cache()[A] = std::make_pair(k, std::move(p));
+  return raw;
+}
+
+SpB_Info run_mxv(SpB_Vector y, const SpB_Matrix A, const SpB_Vector x, Plan* p) {
+  if (!p) return SpB_FAILURE;
+  if (A && ((int64_t)A->row != p->n_rows || (int64_t)A->col != p->n_cols)) {
+    set_error("matrix shape does not match the handle");
+    return SpB_FAILURE;
+  }
+  void *xv = nullptr, *yv = nullptr;
+  if (!host_vector(x, p->type, p->n_cols, &xv) || !host_vector(y, p->type, p->n_rows, &yv)) return SpB_FAILURE;
+  return p->run_host(xv, yv) ? SpB_SUCCESS : SpB_FAILURE;
+}
+
+}  // namespace
+
+extern "C" {
+
+SpB_Info SpB_mxv(SpB_Vector y, const SpB_Matrix A, const SpB_Vector x, void* VNEC) {
+  clear_error();
+  if (!A) {
+    set_error("matrix is NULL");
+    return SpB_FAILURE;
+  }
+  return run_mxv(y, A, x, plan_for_mxv(A, VNEC));
+}
+
+SpB_VNEC_type IRD_VNEC(const SpB_Matrix A, SpB_Type type) {
+  clear_error();
+  CsrView v;
+  if (!view_from_matrix(A, &v) || !validate_csr(v, false)) return SpB_VNEC_S;
+  IrdParams prm = ird_params(type);
+  float ird = ird_ratio(v, prm);
+  return ird >= prm.threshold ? SpB_VNEC_D : SpB_VNEC_S;
+}
+
+struct VNEC_L* Build_VNEC_L(const SpB_Matrix A) {
+  clear_error();
+  CsrView v;
+  if (!view_from_matrix(A, &v)) return nullptr;
+  std::unique_ptr<Plan> plan = build_merge_path(v, nullptr);
+  if (!plan) return nullptr;
+  auto* pub = publish<VNEC_L>(std::move(plan));
+  if (pub) {
+    MpShape sh;
+    int64_t items = v.nnz + v.n_rows;
+    pub->num_merge_items = items > 0x7fffffff ? 0x7fffffff : (int)items;
+    pub->items_per_thread = sh.ipt;
+  }
+  return pub;
+}
+
+void SpMV_VNEC_L_FP64(SpB_Vector y, const SpB_Matrix A, const SpB_Vector x, VNEC_L* mat_thd) {
+  clear_error();
+  Plan* p = find_plan(mat_thd);
+  if (!p) {
+    set_error("SpMV_VNEC_L_FP64: unknown VNEC_L handle");
+    return;
+  }
+  if (p->type != SpB_FP64) {
+    set_error("SpMV_VNEC_L_FP64: handle was built from an FP32 matrix");
+    return;
+  }
+  run_mxv(y, A, x, p);
+}
+
+void SpMV_VNEC_L_FP32(SpB_Vector y, const SpB_Matrix A, const SpB_Vector x, VNEC_L* mat_thd) {
+  clear_error();
+  Plan* p = find_plan(mat_thd);
+  if (!p) {
+    set_error("SpMV_VNEC_L_FP32: unknown VNEC_L handle");
+    return;
+  }
+  if (p->type != SpB_FP32) {
+    set_error("SpMV_VNEC_L_FP32: handle was built from an FP64 matrix");
+    return;
+  }
+  run_mxv(y, A, x, p);
+}
+
+void VNEC_L_free_ext(VNEC_L* mat_thd) { SpB_VNEC_plan_free_ext(mat_thd); }
+
+const char* SpB_VNEC_last_error_ext(void) { return last_error(); }
+
+void* SpB_VNEC_plan_ext(const SpB_VNEC_options_ext* opts, SpB_Type type, int64_t n_rows, int64_t n_cols,
+                        const int64_t* row_ptr, const int32_t* col, const void* val) {
+  clear_error();
+  CsrView v;
+  if (!view_from_arrays(type, n_rows, n_cols, row_ptr, col, val, &v)) return nullptr;
+  std::unique_ptr<Plan> p = build_from_view(v, opts);
+  if (!p) return nullptr;
+  return publish<VNEC_L>(std::move(p));
+}
+
+void* SpB_VNEC_plan_matrix_ext(const SpB_VNEC_options_ext* opts, const SpB_Matrix A) {
+  clear_error();
+  CsrView v;
+  if (!view_from_matrix(A, &v)) return nullptr;
+  std::unique_ptr<Plan> p = build_from_view(v, opts);
+  if (!p) return nullptr;
+  return publish<VNEC_L>(std::move(p));
+}
+
+void SpB_VNEC_plan_free_ext(void* plan) {
+  if (!plan) return;
+  std::unique_ptr<Plan> p = take_plan(plan);
+  if (p) std::free(plan);
+}
+
+void SpB_VNEC_forget_ext(const SpB_Matrix A) {
+  std::lock_guard<std::mutex> g(g_cache_mu);
+  auto_cache().erase(A);
+}
+
+SpB_Info SpB_mxv_device_ext(void* plan, const void* d_x, void* d_y, void* stream) {
+  clear_error();
+  Plan* p = find_plan(plan);
+  if (!p) {
+    set_error("unknown plan");
+    return SpB_FAILURE;
+  }
+  if ((p->n_cols > 0 && !d_x) || (p->n_rows > 0 && !d_y)) {
+    set_error("x or y is NULL");
+    return SpB_FAILURE;
+  }
+  return p->run(d_x, d_y, static_cast<cudaStream_t>(stream)) ? SpB_SUCCESS : SpB_FAILURE;
+}
+
+SpB_Info SpB_mxv_host_ext(void* plan, const void* h_x, void* h_y) {
+  clear_error();
+  Plan* p = find_plan(plan);
+  if (!p) {
+    set_error("unknown plan");
+    return SpB_FAILURE;
+  }
+  if ((p->n_cols > 0 && !h_x) || (p->n_rows > 0 && !h_y)) {
+    set_error("x or y is NULL");
+    return SpB_FAILURE;
+  }
+  return p->run_host(h_x, h_y) ? SpB_SUCCESS : SpB_FAILURE;
+}
+
+SpB_Info SpB_VNEC_plan_info_ext(const void* plan, SpB_VNEC_info_ext* info) {
+  clear_error();
+  Plan* p = find_plan(plan);
+  if (!p || !info) {
+    set_error("unknown plan or NULL info");
+    return SpB_FAILURE;
+  }
+  std::memset(info, 0, sizeof(*info));
+  p->describe(info);
+  info->value_type = p->type;
+  info->n_rows = p->n_rows;
+  info->n_cols = p->n_cols;
+  info->nnz = p->nnz;
+  info->device_bytes = p->device_bytes();
+  info->algorithmic_bytes = p->algorithmic_bytes();
+  info->launches_per_call = p->launches_per_call();
+  return SpB_SUCCESS;
+}
+
+SpB_Info SpB_VNEC_set_profiling_ext(void* plan, int enable) {
+  clear_error();
+  Plan* p = find_plan(plan);
+  if (!p) {
+    set_error("unknown plan");
+    return SpB_FAILURE;
+  }
+  p->profiling = enable != 0;
+  return SpB_SUCCESS;
+}
+
+int SpB_VNEC_kernel_ms_ext(const void* plan, float* ms, int cap) {
+  Plan* p = find_plan(plan);
+  if (!p || !ms) return 0;
+  return p->kernel_ms(ms, cap);
+}
+
+}  // extern "C"

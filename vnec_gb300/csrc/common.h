@@ -1,0 +1,82 @@
+// Internal declarations shared by the host plan code and the CUDA kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstddef>
+#include <cstdint>
+#include <string>
+
+namespace vnec {
+
+// ---------------------------------------------------------------------------
+// Errors: every C-ABI entry point reports failures through SpB_Info and a
+// thread-local message (the reference prints and exit()s instead,
+// src/core/src/SpB_Error.c:4-8).
+// ---------------------------------------------------------------------------
+void set_error(const std::string& msg);
+void clear_error();
+const char* last_error();
+
+bool cuda_ok(cudaError_t e, const char* what);
+#define VNEC_CUDA(call) ::vnec::cuda_ok((call), #call)
+
+// Owning device allocation.
+struct DeviceBuffer {
+  void* ptr = nullptr;
+  size_t bytes = 0;
+  DeviceBuffer() = default;
+  DeviceBuffer(const DeviceBuffer&) = delete;
+  DeviceBuffer& operator=(const DeviceBuffer&) = delete;
+  ~DeviceBuffer() { release(); }
+  bool alloc(size_t n);
+  void release();
+  template <typename T> T* as() const { return static_cast<T*>(ptr); }
+};
+
+// ---------------------------------------------------------------------------
+// Merge-path CSR kernels (the GPU counterpart of VNEC-L,
+// src/operation/src/spmv_vnec_L_for_mxv.c).
+// ---------------------------------------------------------------------------
+
+// Tile shape of the merge-path kernels: threads per CTA x merge items per thread.
+struct MpShape {
+  int tpb = 256;
+  int ipt = 7;
+  int64_t items_per_tile() const { return (int64_t)tpb * ipt; }
+};
+
+// Value/accumulation forms of the merge-path kernel.
+enum class MpForm : int {
+  kF64 = 0,     // FP64 values and x, FP64 accumulation (plain form)
+  kF32 = 1,     // FP32 values and x, FP32 accumulation (the reference's FP32 twin)
+};
+
+// Device arrays describing a CSR matrix prepared for the merge-path kernels.
+// Offsets are int32 when n_rows + nnz < 2^31, else int64 (`wide`).
+struct MpMatrix {
+  int64_t n_rows = 0, n_cols = 0, nnz = 0;
+  bool wide = false;
+  const void* row_end = nullptr;   // n_rows offsets: row_ptr[1..n_rows]
+  const int32_t* col = nullptr;    // nnz column indices
+  const void* val = nullptr;       // nnz values (double or float)
+  const void* tile_row = nullptr;  // num_tiles + 1 merge coordinates (row)
+  const void* tile_nz = nullptr;   // num_tiles + 1 merge coordinates (nonzero)
+  void* carry_row = nullptr;       // num_tiles scratch
+  void* carry_val = nullptr;       // num_tiles scratch
+  int64_t num_tiles = 0;
+  MpShape shape;
+};
+
+// Fills tile_row / tile_nz (device) for the given shape.
+bool mp_partition(const MpMatrix& m, cudaStream_t s);
+// y = A x; x and y are device pointers of the form's value type.  When
+// `events` is non-null, events[0..2] are recorded before the tile kernel,
+// between the tile and fix-up kernels, and after the fix-up kernel.
+bool mp_spmv(const MpMatrix& m, MpForm form, const void* x, void* y, cudaStream_t s,
+             cudaEvent_t* events = nullptr);
+// Dynamic shared memory bytes of one tile for a shape and value size.
+size_t mp_smem_bytes(const MpShape& sh, size_t value_bytes);
+// Kernel launches per mp_spmv call.
+constexpr int kMpLaunchesPerCall = 2;
+
+}  // namespace vnec

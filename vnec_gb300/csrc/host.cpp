@@ -1,0 +1,415 @@
+// Host-side plan machinery: CSR ingestion and validation, the plan registry,
+// the merge-path plan and the IRD selector restated from the reference.
+
+#include "host.h"
+
+#include <omp.h>
+
+#include <algorithm>
+#include <cstring>
+#include <unordered_map>
+
+namespace vnec {
+
+// ---------------------------------------------------------------------------
+// Errors and device buffers
+// ---------------------------------------------------------------------------
+namespace {
+thread_local std::string g_last_error;
+}
+
+void set_error(const std::string& msg) { g_last_error = msg; }
+void clear_error() { g_last_error.clear(); }
+const char* last_error() { return g_last_error.c_str(); }
+
+bool cuda_ok(cudaError_t e, const char* what) {
+  if (e == cudaSuccess) return true;
+  set_error(std::string(what) + ": " + cudaGetErrorString(e));
+  return false;
+}
+
+bool DeviceBuffer::alloc(size_t n) {
+  release();
+  if (n == 0) n = 16;
+  if (!VNEC_CUDA(cudaMalloc(&ptr, n))) {
+    ptr = nullptr;
+    return false;
+  }
+  bytes = n;
+  return true;
+}
+
+void DeviceBuffer::release() {
+  if (ptr) cudaFree(ptr);
+  ptr = nullptr;
+  bytes = 0;
+}
+
+// ---------------------------------------------------------------------------
+// CSR ingestion
+// ---------------------------------------------------------------------------
+bool view_from_matrix(const SpB_Matrix A, CsrView* v) {
+  if (!A) {
+    set_error("matrix is NULL");
+    return false;
+  }
+  auto* m = reinterpret_cast<const SpB_Matrix_CSC_or_CSR*>(A);
+  if (A->format_type != SpB_CSR) {
+    set_error("matrix is not in CSR format (the VNEC path reads CSR, SpB_Global_Option_set_ext)");
+    return false;
+  }
+  if (A->element_type != SpB_FP64 && A->element_type != SpB_FP32) {
+    set_error("matrix element type must be SpB_FP64 or SpB_FP32");
+    return false;
+  }
+  if (m->ptr_len != A->row + 1) {
+    set_error("CSR ptr_len != rows + 1");
+    return false;
+  }
+  v->type = A->element_type;
+  v->n_rows = (int64_t)A->row;
+  v->n_cols = (int64_t)A->col;
+  v->nnz = (int64_t)m->nnz;
+  v->ptr64 = m->ptr;
+  v->idx64 = m->indices;
+  v->ptr = nullptr;
+  v->idx = nullptr;
+  v->val = m->val;
+  if (v->n_rows > 0 && !v->ptr64) {
+    set_error("CSR ptr is NULL");
+    return false;
+  }
+  if (v->nnz > 0 && (!v->idx64 || !v->val)) {
+    set_error("CSR indices or values are NULL");
+    return false;
+  }
+  return true;
+}
+
+bool view_from_arrays(SpB_Type type, int64_t n_rows, int64_t n_cols, const int64_t* row_ptr, const int32_t* col,
+                      const void* val, CsrView* v) {
+  if (type != SpB_FP64 && type != SpB_FP32) {
+    set_error("value type must be SpB_FP64 or SpB_FP32");
+    return false;
+  }
+  if (n_rows < 0 || n_cols < 0 || !row_ptr) {
+    set_error("invalid CSR shape or NULL row_ptr");
+    return false;
+  }
+  v->type = type;
+  v->n_rows = n_rows;
+  v->n_cols = n_cols;
+  v->nnz = row_ptr[n_rows];
+  v->ptr = row_ptr;
+  v->idx = col;
+  v->ptr64 = nullptr;
+  v->idx64 = nullptr;
+  v->val = val;
+  if (v->nnz > 0 && (!col || !val)) {
+    set_error("CSR col or val is NULL");
+    return false;
+  }
+  return true;
+}
+
+bool validate_csr(const CsrView& v, bool need_sorted) {
+  if (v.n_cols > 0x7fffffffLL) {
+    set_error("n_cols must fit in int32");
+    return false;
+  }
+  if (v.row_begin(0) != 0 || v.row_begin(v.n_rows) != v.nnz || v.nnz < 0) {
+    set_error("CSR offsets must start at 0 and end at nnz");
+    return false;
+  }
+  int bad = 0;
+#pragma omp parallel for schedule(static) reduction(| : bad)
+  for (int64_t r = 0; r < v.n_rows; ++r) {
+    int64_t b = v.row_begin(r), e = v.row_begin(r + 1);
+    if (e < b || e > v.nnz) {
+      bad |= 1;
+      continue;
+    }
+    int64_t prev = -1;
+    for (int64_t p = b; p < e; ++p) {
+      int64_t c = v.col_at(p);
+      if (c < 0 || c >= v.n_cols) bad |= 2;
+      if (need_sorted && c <= prev) bad |= 4;
+      prev = c;
+    }
+  }
+  if (bad & 1) {
+    set_error("CSR offsets are not monotone");
+    return false;
+  }
+  if (bad & 2) {
+    set_error("CSR column index out of range");
+    return false;
+  }
+  if (bad & 4) {
+    set_error("CSR columns are not strictly increasing within a row");
+    return false;
+  }
+  return true;
+}
+
+void convert_row_end(const CsrView& v, bool wide, void* out) {
+  if (wide) {
+    auto* o = static_cast<int64_t*>(out);
+#pragma omp parallel for schedule(static)
+    for (int64_t r = 0; r < v.n_rows; ++r) o[r] = v.row_begin(r + 1);
+  } else {
+    auto* o = static_cast<int32_t*>(out);
+#pragma omp parallel for schedule(static)
+    for (int64_t r = 0; r < v.n_rows; ++r) o[r] = (int32_t)v.row_begin(r + 1);
+  }
+}
+
+void convert_cols(const CsrView& v, int32_t* out) {
+  if (v.idx) {
+    std::memcpy(out, v.idx, sizeof(int32_t) * (size_t)v.nnz);
+    return;
+  }
+#pragma omp parallel for schedule(static)
+  for (int64_t p = 0; p < v.nnz; ++p) out[p] = (int32_t)v.idx64[p];
+}
+
+// ---------------------------------------------------------------------------
+// Plans and registry
+// ---------------------------------------------------------------------------
+Plan::~Plan() {
+  if (own_stream) cudaStreamDestroy(own_stream);
+  for (cudaEvent_t& e : events)
+    if (e) cudaEventDestroy(e);
+}
+
+bool Plan::ensure_events() {
+  for (cudaEvent_t& e : events)
+    if (!e && !VNEC_CUDA(cudaEventCreate(&e))) return false;
+  return true;
+}
+
+bool Plan::run_host(const void* h_x, void* h_y) {
+  const size_t vb = type == SpB_FP64 ? 8 : 4;
+  if (!own_stream && !VNEC_CUDA(cudaStreamCreateWithFlags(&own_stream, cudaStreamNonBlocking))) return false;
+  if (!dx.ptr && !dx.alloc(vb * (size_t)std::max<int64_t>(n_cols, 1))) return false;
+  if (!dy.ptr && !dy.alloc(vb * (size_t)std::max<int64_t>(n_rows, 1))) return false;
+  if (n_cols > 0 && !VNEC_CUDA(cudaMemcpyAsync(dx.ptr, h_x, vb * n_cols, cudaMemcpyHostToDevice, own_stream)))
+    return false;
+  if (!run(dx.ptr, dy.ptr, own_stream)) return false;
+  if (n_rows > 0 && !VNEC_CUDA(cudaMemcpyAsync(h_y, dy.ptr, vb * n_rows, cudaMemcpyDeviceToHost, own_stream)))
+    return false;
+  return VNEC_CUDA(cudaStreamSynchronize(own_stream));
+}
+
+namespace {
+std::mutex g_reg_mu;
+std::unordered_map<const void*, std::unique_ptr<Plan>>& registry() {
+  static auto* r = new std::unordered_map<const void*, std::unique_ptr<Plan>>();
+  return *r;
+}
+}  // namespace
+
+void register_plan(const void* handle, std::unique_ptr<Plan> plan) {
+  std::lock_guard<std::mutex> g(g_reg_mu);
+  registry()[handle] = std::move(plan);
+}
+
+Plan* find_plan(const void* handle) {
+  std::lock_guard<std::mutex> g(g_reg_mu);
+  auto it = registry().find(handle);
+  return it == registry().end() ? nullptr : it->second.get();
+}
+
+std::unique_ptr<Plan> take_plan(const void* handle) {
+  std::lock_guard<std::mutex> g(g_reg_mu);
+  auto it = registry().find(handle);
+  if (it == registry().end()) return nullptr;
+  std::unique_ptr<Plan> p = std::move(it->second);
+  registry().erase(it);
+  return p;
+}
+
+// ---------------------------------------------------------------------------
+// Merge-path plan (VNEC-L counterpart)
+// ---------------------------------------------------------------------------
+namespace {
+
+struct MergePathPlan final : Plan {
+  MpMatrix m;
+  DeviceBuffer row_end, col, val, tile_row, tile_nz, carry_row, carry_val;
+  MergePathPlan() : Plan(PlanKind::kMergePath) {}
+  bool run(const void* d_x, void* d_y, cudaStream_t s) override {
+    if (profiling && !ensure_events()) return false;
+    return mp_spmv(m, type == SpB_FP64 ? MpForm::kF64 : MpForm::kF32, d_x, d_y, s,
+                   profiling ? events : nullptr);
+  }
+  int kernel_ms(float* ms, int cap) const override {
+    if (!profiling || !events[0] || cap < 2) return 0;
+    if (cudaEventSynchronize(events[2]) != cudaSuccess) return 0;
+    cudaEventElapsedTime(&ms[0], events[0], events[1]);
+    cudaEventElapsedTime(&ms[1], events[1], events[2]);
+    return 2;
+  }
+  int launches_per_call() const override { return n_rows > 0 ? kMpLaunchesPerCall : 0; }
+  int64_t device_bytes() const override {
+    return (int64_t)(row_end.bytes + col.bytes + val.bytes + tile_row.bytes + tile_nz.bytes + carry_row.bytes +
+                     carry_val.bytes + dx.bytes + dy.bytes);
+  }
+  int64_t algorithmic_bytes() const override {
+    const int64_t vb = type == SpB_FP64 ? 8 : 4, ob = m.wide ? 8 : 4;
+    return nnz * (vb + 4) + (n_rows + 1) * ob + n_cols * vb + n_rows * vb;
+  }
+  void describe(SpB_VNEC_info_ext* info) const override {
+    info->kernel = SpB_VNEC_KERNEL_L;
+    info->threads_per_block = m.shape.tpb;
+    info->items_per_thread = m.shape.ipt;
+    info->num_tiles = m.num_tiles;
+  }
+};
+
+bool shape_supported(int tpb, int ipt) {
+  return (tpb == 128 || tpb == 256) && (ipt == 4 || ipt == 7 || ipt == 10);
+}
+
+}  // namespace
+
+std::unique_ptr<Plan> build_merge_path(const CsrView& v, const SpB_VNEC_options_ext* opts) {
+  if (!validate_csr(v, false)) return nullptr;
+  auto p = std::make_unique<MergePathPlan>();
+  p->type = v.type;
+  p->n_rows = v.n_rows;
+  p->n_cols = v.n_cols;
+  p->nnz = v.nnz;
+  cudaGetDevice(&p->device);
+  MpShape sh;
+  if (opts && opts->threads_per_block) sh.tpb = opts->threads_per_block;
+  if (opts && opts->items_per_thread) sh.ipt = opts->items_per_thread;
+  if (!shape_supported(sh.tpb, sh.ipt)) {
+    set_error("unsupported merge-path tile shape (threads 128/256, items 4/7/10)");
+    return nullptr;
+  }
+  MpMatrix& m = p->m;
+  m.n_rows = v.n_rows;
+  m.n_cols = v.n_cols;
+  m.nnz = v.nnz;
+  m.shape = sh;
+  m.wide = (v.n_rows + v.nnz) >= ((int64_t)1 << 31) - 1;
+  const size_t ob = m.wide ? 8 : 4;
+  const size_t vb = v.value_bytes();
+  const int64_t ipc = sh.items_per_tile();
+  m.num_tiles = (v.n_rows + v.nnz + ipc - 1) / ipc;
+  // Device arrays are padded by 16 elements so that vector loads near the end
+  // stay inside the allocation.
+  const size_t pad = 16;
+  if (!p->row_end.alloc(ob * (v.n_rows + pad)) || !p->col.alloc(4 * (v.nnz + pad)) ||
+      !p->val.alloc(vb * (v.nnz + pad)) || !p->tile_row.alloc(ob * (m.num_tiles + 1)) ||
+      !p->tile_nz.alloc(ob * (m.num_tiles + 1)) || !p->carry_row.alloc(ob * (m.num_tiles + 1)) ||
+      !p->carry_val.alloc(vb * (m.num_tiles + 1)))
+    return nullptr;
+  {
+    std::vector<unsigned char> host_end(ob * (size_t)std::max<int64_t>(v.n_rows, 1));
+    convert_row_end(v, m.wide, host_end.data());
+    if (v.n_rows && !VNEC_CUDA(cudaMemcpy(p->row_end.ptr, host_end.data(), ob * v.n_rows, cudaMemcpyHostToDevice)))
+      return nullptr;
+  }
+  if (v.nnz) {
+    if (v.idx) {
+      if (!VNEC_CUDA(cudaMemcpy(p->col.ptr, v.idx, 4 * v.nnz, cudaMemcpyHostToDevice))) return nullptr;
+    } else {
+      std::vector<int32_t> host_col((size_t)v.nnz);
+      convert_cols(v, host_col.data());
+      if (!VNEC_CUDA(cudaMemcpy(p->col.ptr, host_col.data(), 4 * v.nnz, cudaMemcpyHostToDevice))) return nullptr;
+    }
+    if (!VNEC_CUDA(cudaMemcpy(p->val.ptr, v.val, vb * v.nnz, cudaMemcpyHostToDevice))) return nullptr;
+  }
+  // Zero the padding so no uninitialised value is ever read.
+  if (!VNEC_CUDA(cudaMemset(p->col.as<char>() + 4 * v.nnz, 0, 4 * pad)) ||
+      !VNEC_CUDA(cudaMemset(p->val.as<char>() + vb * v.nnz, 0, vb * pad)))
+    return nullptr;
+  m.row_end = p->row_end.ptr;
+  m.col = p->col.as<int32_t>();
+  m.val = p->val.ptr;
+  m.tile_row = p->tile_row.ptr;
+  m.tile_nz = p->tile_nz.ptr;
+  m.carry_row = p->carry_row.ptr;
+  m.carry_val = p->carry_val.ptr;
+  if (v.n_rows > 0) {
+    if (!mp_partition(m, nullptr)) return nullptr;
+    if (!VNEC_CUDA(cudaDeviceSynchronize())) return nullptr;
+  }
+  return p;
+}
+
+// ---------------------------------------------------------------------------
+// IRD selector (ird_calc.c:2-122), restated for a host CSR view.
+// ---------------------------------------------------------------------------
+IrdParams ird_params(SpB_Type type) {
+  // Constants of the reference's X86_SIMD build (SpB_mxv.h:25-32).
+  if (type == SpB_FP32) return IrdParams{36, 16, 0.437f};
+  return IrdParams{36, 8, 0.477f};
+}
+
+namespace {
+// MergePathDivide (spmv_vnec_common.c:3-33) on a host view.
+void merge_divide(const CsrView& v, int64_t diag, int64_t* x, int64_t* y) {
+  int64_t lo = std::max<int64_t>(diag - v.nnz, 0), hi = std::min<int64_t>(diag, v.n_rows);
+  while (lo < hi) {
+    int64_t p = (lo + hi) >> 1;
+    if (v.row_begin(p + 1) <= diag - p - 1)
+      lo = p + 1;
+    else
+      hi = p;
+  }
+  *x = std::min<int64_t>(lo, v.n_rows);
+  *y = diag - lo;
+}
+}  // namespace
+
+float ird_ratio(const CsrView& v, const IrdParams& prm) {
+  const int P = prm.nparts;
+  std::vector<int64_t> sx(P), sy(P), ex(P), ey(P);
+  const int64_t items = v.nnz + v.n_rows, per = (items + P - 1) / P;
+  for (int t = 0; t < P; ++t) {
+    int64_t d0 = std::min(per * t, items), d1 = std::min(d0 + per, items);
+    merge_divide(v, d0, &sx[t], &sy[t]);
+    merge_divide(v, d1, &ex[t], &ey[t]);
+  }
+  const int64_t words = (v.n_cols + 63) / 64;
+  int64_t blocks_total = 0;
+#pragma omp parallel for schedule(dynamic, 1) reduction(+ : blocks_total)
+  for (int t = 0; t < P; ++t) {
+    // ECR ranks: rank of a column among the distinct columns of the partition.
+    std::vector<uint64_t> bits((size_t)words, 0);
+    for (int64_t p = sy[t]; p < ey[t]; ++p) {
+      int64_t c = v.col_at(p);
+      bits[c >> 6] |= 1ull << (c & 63);
+    }
+    std::vector<int32_t> base((size_t)words + 1, 0);
+    for (int64_t w = 0; w < words; ++w) base[w + 1] = base[w] + __builtin_popcountll(bits[w]);
+    auto rank = [&](int64_t c) -> int64_t {
+      uint64_t below = bits[c >> 6] & ((1ull << (c & 63)) - 1);
+      return base[c >> 6] + __builtin_popcountll(below);
+    };
+    // Block grouping of the complete rows (ird_calc.c:72-101).
+    int64_t g = 0;
+    for (int64_t i = sx[t]; i < ex[t]; ++i) {
+      int64_t p0 = std::max(v.row_begin(i), sy[t]);
+      int64_t len = v.row_begin(i + 1) - p0;
+      if (len <= 0) continue;
+      int64_t cs = rank(v.col_at(p0));
+      for (int64_t j = 1; j < len; ++j) {
+        int64_t r = rank(v.col_at(p0 + j));
+        if (r - cs >= prm.nlanes) {
+          ++g;
+          cs = r;
+        }
+      }
+      ++g;
+    }
+    blocks_total += g;
+  }
+  const int denom = (int)(blocks_total * prm.nlanes);
+  return (float)v.nnz / (float)denom;
+}
+
+}  // namespace vnec

@@ -1,0 +1,89 @@
+// Host-side plan machinery shared by the C-ABI translation units.
+#pragma once
+
+#include <cstdint>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "common.h"
+#include "vnec_gb300.h"
+
+namespace vnec {
+
+// A CSR matrix as handed in by a caller: either the reference's
+// SpB_Matrix_CSC_or_CSR (64-bit offsets and columns) or raw arrays (int64
+// offsets, int32 columns).
+struct CsrView {
+  SpB_Type type = SpB_FP64;
+  int64_t n_rows = 0, n_cols = 0, nnz = 0;
+  const SpB_Index* ptr64 = nullptr;  // reference layout
+  const SpB_Index* idx64 = nullptr;
+  const int64_t* ptr = nullptr;      // raw layout
+  const int32_t* idx = nullptr;
+  const void* val = nullptr;
+  int64_t row_begin(int64_t r) const { return ptr64 ? (int64_t)ptr64[r] : ptr[r]; }
+  int64_t col_at(int64_t p) const { return idx64 ? (int64_t)idx64[p] : idx[p]; }
+  size_t value_bytes() const { return type == SpB_FP64 ? 8 : 4; }
+};
+
+bool view_from_matrix(const SpB_Matrix A, CsrView* v);
+bool view_from_arrays(SpB_Type type, int64_t n_rows, int64_t n_cols, const int64_t* row_ptr, const int32_t* col,
+                      const void* val, CsrView* v);
+// Checks ptr[0]==0, monotone offsets, ptr[n]==nnz, 0<=col<n_cols (and, when
+// `need_sorted`, strictly increasing columns per row).
+bool validate_csr(const CsrView& v, bool need_sorted);
+// Row ends (row_ptr[1..n]) as int32 or int64 and int32 columns.
+void convert_row_end(const CsrView& v, bool wide, void* out);
+void convert_cols(const CsrView& v, int32_t* out);
+
+// Kinds of plans this library builds.
+enum class PlanKind : int { kMergePath = 1, kWindowDense = 2, kWindowSliced = 3, kMixed = 4 };
+
+// Base of every plan.  The reference-typed public struct handed to callers is
+// a separate calloc'd block registered against the plan (see registry below).
+struct Plan {
+  PlanKind kind;
+  SpB_Type type = SpB_FP64;  // value type of x and y
+  int64_t n_rows = 0, n_cols = 0, nnz = 0;
+  int device = 0;
+  cudaStream_t own_stream = nullptr;
+  DeviceBuffer dx, dy;  // staging for host-vector calls
+  // Per-kernel timing of the most recent call (SpB_VNEC_set_profiling_ext).
+  bool profiling = false;
+  cudaEvent_t events[4] = {nullptr, nullptr, nullptr, nullptr};
+  bool ensure_events();
+  explicit Plan(PlanKind k) : kind(k) {}
+  virtual ~Plan();
+  virtual bool run(const void* d_x, void* d_y, cudaStream_t s) = 0;
+  virtual int launches_per_call() const = 0;
+  virtual int64_t device_bytes() const = 0;
+  // Algorithmic bytes moved by one call (roofline numerator).
+  virtual int64_t algorithmic_bytes() const = 0;
+  // Kernel-specific fields of SpB_VNEC_info_ext.
+  virtual void describe(SpB_VNEC_info_ext* info) const = 0;
+  // Milliseconds of each kernel of the last profiled call (main kernel first).
+  virtual int kernel_ms(float* ms, int cap) const = 0;
+  bool run_host(const void* h_x, void* h_y);
+};
+
+// Registry: public handle pointer -> plan.
+void register_plan(const void* handle, std::unique_ptr<Plan> plan);
+Plan* find_plan(const void* handle);
+std::unique_ptr<Plan> take_plan(const void* handle);
+
+// Plan builders.
+std::unique_ptr<Plan> build_merge_path(const CsrView& v, const SpB_VNEC_options_ext* opts);
+
+// Reference partition count and lane width constants used by IRD_VNEC.
+struct IrdParams {
+  int nparts;
+  int nlanes;
+  float threshold;
+};
+IrdParams ird_params(SpB_Type type);
+// IRD = nnz / (blocks * nlanes) as IRD_VNEC computes it (ird_calc.c:2-122).
+float ird_ratio(const CsrView& v, const IrdParams& p);
+
+}  // namespace vnec

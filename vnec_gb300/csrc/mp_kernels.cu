@@ -1,0 +1,263 @@
+// Merge-path CSR SpMV for sm_103a — the GPU counterpart of VNEC-L
+// (src/operation/src/spmv_vnec_L_for_mxv.c:124-165) and of its partitioner
+// MergePathDivide (src/operation/src/spmv_vnec_common.c:3-33).
+//
+// Work decomposition.  The merge of the row-end list (row_ptr[1..n]) and the
+// nonzero counting list (0..nnz-1) has n_rows + nnz items.  It is cut into
+// tiles of TPB*IPT items, one CTA per tile; the tile boundaries are found once
+// per matrix (plan time) by mp_partition_kernel.  Inside a tile:
+//   1. stage: the tile's values, the gathered x[col] and its row ends are
+//      copied to shared memory with coalesced loads (values and columns are
+//      read once, so they are loaded with the streaming cache hint; x is
+//      gathered through the read-only path so it stays resident in L2);
+//   2. consume: each thread runs the merge path over IPT consecutive items of
+//      the tile — one FMA per nonzero, a row result at each row end — exactly
+//      the per-thread loop of the reference's OpenMP threads, at warp lane
+//      granularity;
+//   3. carry: a thread whose segment starts inside a row adds the partial sums
+//      of the preceding threads that stopped in the same row (a walk back over
+//      the shared carry list, one add per carried partial), then writes that
+//      row; the tile's own carry-out (partial of its last row) goes to a
+//      per-tile scratch slot;
+//   4. fix-up (second, tiny launch): rows spanning tiles receive the ordered
+//      sum of the carries of the tiles that stopped inside them — the
+//      counterpart of the reference's serial carry loop (:159-164).
+// The FP64 form performs exactly one FP64 FMA per nonzero plus one add per
+// carried partial: on GB300 the FP64 pipe (about 0.6 T FMA/s) is close to the
+// HBM rate for SpMV, so no other FP64 work is done in the loop.
+
+#include <cuda_runtime.h>
+#include <cstdint>
+
+#include "common.h"
+
+namespace vnec {
+namespace {
+
+template <typename T> __device__ __forceinline__ T ld_stream(const T* p) { return __ldcs(p); }
+__device__ __forceinline__ long long ld_stream(const long long* p) { return __ldcs(p); }
+
+template <typename V> __device__ __forceinline__ V fma_v(V a, V b, V c);
+template <> __device__ __forceinline__ double fma_v<double>(double a, double b, double c) { return fma(a, b, c); }
+template <> __device__ __forceinline__ float fma_v<float>(float a, float b, float c) { return fmaf(a, b, c); }
+
+// Diagonal search of one merge-path boundary (MergePathDivide semantics:
+// move right while row_end[pivot] <= diag - pivot - 1).
+template <typename Off>
+__device__ __forceinline__ Off merge_search(const Off* row_end, Off diag, Off n_rows, Off nnz) {
+  Off lo = diag - nnz > 0 ? diag - nnz : 0;
+  Off hi = diag < n_rows ? diag : n_rows;
+  while (lo < hi) {
+    Off p = (lo + hi) >> 1;
+    if (row_end[p] <= diag - p - 1)
+      lo = p + 1;
+    else
+      hi = p;
+  }
+  return lo;
+}
+
+template <typename Off>
+__global__ void mp_partition_kernel(const Off* __restrict__ row_end, Off n_rows, Off nnz, long long ipc,
+                                    long long num_tiles, Off* __restrict__ tile_row, Off* __restrict__ tile_nz) {
+  long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t > num_tiles) return;
+  Off total = n_rows + nnz;
+  long long d64 = t * ipc;
+  Off diag = d64 < (long long)total ? (Off)d64 : total;
+  Off r = merge_search<Off>(row_end, diag, n_rows, nnz);
+  tile_row[t] = r;
+  tile_nz[t] = diag - r;
+}
+
+// One CTA per tile.  Shared memory: s_val[IPC], s_x[IPC] (V), s_carry[TPB] (V),
+// s_end[IPC] (int, row ends relative to the tile's first nonzero), s_emit[TPB].
+template <typename V, typename Off, int TPB, int IPT>
+__global__ void __launch_bounds__(TPB)
+mp_spmv_kernel(const Off* __restrict__ row_end, const int32_t* __restrict__ col, const V* __restrict__ val,
+               const V* __restrict__ x, V* __restrict__ y, const Off* __restrict__ tile_row,
+               const Off* __restrict__ tile_nz, Off* __restrict__ carry_row, V* __restrict__ carry_val) {
+  constexpr int IPC = TPB * IPT;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  V* s_val = reinterpret_cast<V*>(smem_raw);
+  V* s_x = s_val + IPC;
+  V* s_carry = s_x + IPC;
+  int* s_end = reinterpret_cast<int*>(s_carry + TPB);
+  int* s_emit = s_end + IPC;
+
+  const int tile = blockIdx.x;
+  const int tid = threadIdx.x;
+  const Off x0 = tile_row[tile], y0 = tile_nz[tile];
+  const Off x1 = tile_row[tile + 1], y1 = tile_nz[tile + 1];
+  const int nrows = (int)(x1 - x0);
+  const int nnz = (int)(y1 - y0);
+
+  // 1. stage values, gathered x and row ends.
+  {
+    const int32_t* c_t = col + y0;
+    const V* v_t = val + y0;
+#pragma unroll 4
+    for (int i = tid; i < nnz; i += TPB) {
+      int c = ld_stream(c_t + i);
+      s_val[i] = ld_stream(v_t + i);
+      s_x[i] = __ldg(x + c);
+    }
+    const Off* e_t = row_end + x0;
+    for (int i = tid; i < nrows; i += TPB) s_end[i] = (int)(ld_stream(e_t + i) - y0);
+  }
+  __syncthreads();
+
+  // 2. per-thread merge path over IPT items.
+  const int total = nrows + nnz;
+  const int d = min(tid * IPT, total);
+  int rr = merge_search<int>(s_end, d, nrows, nnz);
+  int kk = d - rr;
+  const int dend = min(d + IPT, total);
+  V acc = V(0);
+  V first_val = V(0);
+  int first = -1;
+#pragma unroll
+  for (int it = 0; it < IPT; ++it) {
+    if (d + it < dend) {
+      if (rr < nrows && s_end[rr] <= kk) {
+        if (first < 0) {
+          first = rr;
+          first_val = acc;
+        } else {
+          y[x0 + rr] = acc;
+        }
+        acc = V(0);
+        ++rr;
+      } else {
+        acc = fma_v<V>(s_val[kk], s_x[kk], acc);
+        ++kk;
+      }
+    }
+  }
+  s_carry[tid] = acc;
+  s_emit[tid] = first >= 0;
+  __syncthreads();
+
+  // 3. in-tile carries: sum partials of preceding threads that stopped in the
+  // row this thread starts in (they form a run ending at a thread that
+  // emitted a row, or at thread 0).
+  if (first >= 0) {
+    V c = V(0);
+    for (int u = tid - 1; u >= 0; --u) {
+      c += s_carry[u];
+      if (s_emit[u]) break;
+    }
+    y[x0 + first] = first_val + c;
+  }
+  if (tid == TPB - 1) {
+    V c = V(0);
+    for (int u = TPB - 1; u >= 0; --u) {
+      c += s_carry[u];
+      if (s_emit[u]) break;
+    }
+    carry_row[tile] = x1;
+    carry_val[tile] = c;
+  }
+}
+
+// 4. cross-tile carries: the first tile of each run of tiles that stopped in
+// the same row adds the run's carries, in tile order, to that row.
+template <typename V, typename Off>
+__global__ void mp_fixup_kernel(const Off* __restrict__ carry_row, const V* __restrict__ carry_val,
+                                long long num_tiles, Off n_rows, V* __restrict__ y) {
+  long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= num_tiles) return;
+  Off r = carry_row[t];
+  if (r >= n_rows) return;
+  if (t > 0 && carry_row[t - 1] == r) return;
+  V s = V(0);
+  for (long long u = t; u < num_tiles && carry_row[u] == r; ++u) s += carry_val[u];
+  y[r] += s;
+}
+
+template <typename V, typename Off, int TPB, int IPT>
+bool launch_mp(const MpMatrix& m, const void* x, void* y, cudaStream_t s, cudaEvent_t* ev) {
+  auto kern = mp_spmv_kernel<V, Off, TPB, IPT>;
+  MpShape sh;
+  sh.tpb = TPB;
+  sh.ipt = IPT;
+  size_t smem = mp_smem_bytes(sh, sizeof(V));
+  static bool configured = false;  // per instantiation
+  if (!configured) {
+    if (!VNEC_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)))
+      return false;
+    configured = true;
+  }
+  if (m.num_tiles > 0x7fffffffLL) {
+    set_error("merge-path: tile count exceeds the grid limit");
+    return false;
+  }
+  if (ev && !VNEC_CUDA(cudaEventRecord(ev[0], s))) return false;
+  kern<<<(unsigned)m.num_tiles, TPB, smem, s>>>(
+      static_cast<const Off*>(m.row_end), m.col, static_cast<const V*>(m.val), static_cast<const V*>(x),
+      static_cast<V*>(y), static_cast<const Off*>(m.tile_row), static_cast<const Off*>(m.tile_nz),
+      static_cast<Off*>(m.carry_row), static_cast<V*>(m.carry_val));
+  if (!VNEC_CUDA(cudaGetLastError())) return false;
+  if (ev && !VNEC_CUDA(cudaEventRecord(ev[1], s))) return false;
+  const int fb = 256;
+  long long fg = (m.num_tiles + fb - 1) / fb;
+  mp_fixup_kernel<V, Off><<<(unsigned)fg, fb, 0, s>>>(static_cast<const Off*>(m.carry_row),
+                                                      static_cast<const V*>(m.carry_val), m.num_tiles,
+                                                      (Off)m.n_rows, static_cast<V*>(y));
+  if (!VNEC_CUDA(cudaGetLastError())) return false;
+  if (ev && !VNEC_CUDA(cudaEventRecord(ev[2], s))) return false;
+  return true;
+}
+
+template <typename V, typename Off>
+bool dispatch_shape(const MpMatrix& m, const void* x, void* y, cudaStream_t s, cudaEvent_t* ev) {
+  const int tpb = m.shape.tpb, ipt = m.shape.ipt;
+#define VNEC_MP_CASE(T, I) \
+  if (tpb == T && ipt == I) return launch_mp<V, Off, T, I>(m, x, y, s, ev);
+  VNEC_MP_CASE(128, 4)
+  VNEC_MP_CASE(128, 7)
+  VNEC_MP_CASE(128, 10)
+  VNEC_MP_CASE(256, 4)
+  VNEC_MP_CASE(256, 7)
+  VNEC_MP_CASE(256, 10)
+#undef VNEC_MP_CASE
+  set_error("merge-path: unsupported tile shape");
+  return false;
+}
+
+}  // namespace
+
+size_t mp_smem_bytes(const MpShape& sh, size_t value_bytes) {
+  size_t ipc = (size_t)sh.tpb * sh.ipt;
+  return 2 * ipc * value_bytes + (size_t)sh.tpb * value_bytes + ipc * sizeof(int) + (size_t)sh.tpb * sizeof(int);
+}
+
+bool mp_partition(const MpMatrix& m, cudaStream_t s) {
+  long long ipc = m.shape.items_per_tile();
+  const int b = 256;
+  long long g = (m.num_tiles + 1 + b - 1) / b;
+  if (m.wide) {
+    mp_partition_kernel<long long><<<(unsigned)g, b, 0, s>>>(
+        static_cast<const long long*>(m.row_end), (long long)m.n_rows, (long long)m.nnz, ipc, m.num_tiles,
+        static_cast<long long*>(const_cast<void*>(m.tile_row)), static_cast<long long*>(const_cast<void*>(m.tile_nz)));
+  } else {
+    mp_partition_kernel<int><<<(unsigned)g, b, 0, s>>>(
+        static_cast<const int*>(m.row_end), (int)m.n_rows, (int)m.nnz, ipc, m.num_tiles,
+        static_cast<int*>(const_cast<void*>(m.tile_row)), static_cast<int*>(const_cast<void*>(m.tile_nz)));
+  }
+  return VNEC_CUDA(cudaGetLastError());
+}
+
+bool mp_spmv(const MpMatrix& m, MpForm form, const void* x, void* y, cudaStream_t s, cudaEvent_t* ev) {
+  if (m.n_rows == 0) return true;
+  switch (form) {
+    case MpForm::kF64:
+      return m.wide ? dispatch_shape<double, long long>(m, x, y, s, ev) : dispatch_shape<double, int>(m, x, y, s, ev);
+    case MpForm::kF32:
+      return m.wide ? dispatch_shape<float, long long>(m, x, y, s, ev) : dispatch_shape<float, int>(m, x, y, s, ev);
+  }
+  set_error("merge-path: unknown value form");
+  return false;
+}
+
+}  // namespace vnec
