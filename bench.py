@@ -58,6 +58,10 @@ def workload(name: str):
         m = G.uniform_k(65536, 16, seed=0)
         x = G.vector(m.n_cols, seed=0)
         desc = "uniform_n65536_k16_fp64"
+    elif name == "rmat22":
+        m = G.rmat(22, 1 << 26, 0.57, 0.19, 0.19, seed=1)
+        x = G.vector(m.n_cols, lo=-1.0, hi=1.0, seed=1)
+        desc = "rmat_scale22_edges2^26_a.57_b.19_c.19_dedup_fp64"
     elif name == "stencil256":
         m = G.stencil27(256, seed=0)
         x = G.vector(m.n_cols, seed=0)
@@ -331,7 +335,7 @@ def main() -> None:
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", default="rmat24", choices=["rmat24", "uniform64k", "stencil256"])
+    ap.add_argument("--workload", default="rmat24", choices=["rmat24", "rmat22", "uniform64k", "stencil256"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-budget", type=float, default=20.0, help="seconds of CPU-baseline timing")
     args = ap.parse_args()

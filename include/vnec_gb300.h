@@ -80,11 +80,22 @@ typedef enum {
   SpB_VNEC_KERNEL_S = 3  /* windowed sliced rows */
 } SpB_VNEC_kernel_ext;
 
+/* Arithmetic of the FP64 merge-path kernel. */
+typedef enum {
+  SpB_VNEC_ARITH_AUTO = 0, /* DF32 when A's values allow it, else FP64 */
+  SpB_VNEC_ARITH_FP64 = 1, /* one FP64 FMA per nonzero */
+  SpB_VNEC_ARITH_DF32 = 2  /* double-float on the FP32 pipe: products and sums
+                              with ~2^-46 relative error, needs |a|,|x| in
+                              [2^-40, 2^41) or 0, else the call runs in FP64 */
+} SpB_VNEC_arith_ext;
+
 typedef struct {
   int kernel;            /* SpB_VNEC_kernel_ext */
   int threads_per_block; /* 0: default */
   int items_per_thread;  /* 0: default */
-  int reserved[13];
+  int pipeline_stages;   /* merge-path: 0 default (2), 1 unpipelined kernel, 2-3 stages */
+  int arithmetic;        /* SpB_VNEC_arith_ext (FP64 values) */
+  int reserved[11];
 } SpB_VNEC_options_ext;
 
 /* Plan from raw host CSR arrays: int64 row offsets (n_rows + 1), int32
@@ -121,8 +132,15 @@ typedef struct {
   int threads_per_block;
   int items_per_thread;
   int64_t num_tiles;
-  int reserved[8];
+  int pipeline_stages;     /* 0 for the unpipelined kernel */
+  int arithmetic;          /* SpB_VNEC_arith_ext in use */
+  int reserved[6];
 } SpB_VNEC_info_ext;
+
+/* Device-side error status of the plan's last calls: waits for the plan's
+ * work on `stream`, returns SpB_FAILURE (with a message) if a bounded
+ * pipeline wait timed out, and clears the status. */
+SpB_Info SpB_VNEC_device_status_ext(void *plan, void *stream);
 
 SpB_Info SpB_VNEC_plan_info_ext(const void *plan, SpB_VNEC_info_ext *info);
 

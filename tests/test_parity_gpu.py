@@ -96,18 +96,72 @@ def test_spb_mxv_auto_plan_and_cache(built):
     api.lib().SpB_VNEC_forget_ext(A.handle)
 
 
-@pytest.mark.parametrize("tpb,ipt", [(128, 4), (128, 7), (128, 10), (256, 4), (256, 7), (256, 10)])
-def test_tile_shapes(built, tpb, ipt):
+UNPIPELINED = [(128, 4), (128, 7), (128, 10), (256, 4), (256, 7), (256, 10)]
+PIPELINED = [(256, 7, 2), (256, 7, 3), (256, 12, 2), (128, 12, 3), (512, 5, 2)]
+
+
+def variant_opts():
+    """(label, options) of every FP64 merge-path kernel variant."""
+    from vnec_gb300 import api
+
+    out = [(f"simple{t}x{i}", dict(threads_per_block=t, items_per_thread=i, pipeline_stages=1))
+           for t, i in UNPIPELINED]
+    for t, i, st in PIPELINED:
+        for ar, name in ((api.ARITH_FP64, "f64"), (api.ARITH_DF32, "df32")):
+            out.append((f"pipe{t}x{i}s{st}_{name}", dict(threads_per_block=t, items_per_thread=i,
+                                                         pipeline_stages=st, arithmetic=ar)))
+    return out
+
+
+@pytest.mark.parametrize("label,kw", variant_opts(), ids=[v[0] for v in variant_opts()])
+def test_kernel_variants(built, label, kw):
     from vnec_gb300 import api
     from vnec_gb300 import generators as G
 
-    for m in (G.rmat(16, 16 << 16, seed=7), G.lognormal(20000, sigma=2.5, cap=4096, seed=8)):
+    for m in (G.rmat(16, 16 << 16, seed=7), G.lognormal(20000, sigma=2.5, cap=4096, seed=8),
+              G.stencil27(20, seed=9)):
         xv = G.vector(m.n_cols, seed=9)
-        p = api.Plan(m, kernel=api.KERNEL_L, threads_per_block=tpb, items_per_thread=ipt)
+        p = api.Plan(m, kernel=api.KERNEL_L, **kw)
+        inf = p.info()
+        assert inf.num_tiles == -(-(m.n_rows + m.nnz) // (kw["threads_per_block"] * kw["items_per_thread"]))
         y = p.mxv_host(xv)
         check_f64(y, m, xv)
-        assert p.info().num_tiles == -(-(m.n_rows + m.nnz) // (tpb * ipt))
+        assert p.mxv_host(xv).tobytes() == y.tobytes()  # deterministic
+        p.device_status()
         p.free()
+
+
+def test_df32_falls_back_to_fp64_for_out_of_range_x(built):
+    """An x outside the double-float range raises the device flag; the guard
+    launch recomputes the call in FP64, the next call is back on DF32."""
+    from vnec_gb300 import api
+    from vnec_gb300 import generators as G
+
+    m = G.rmat(15, 16 << 15, seed=3)
+    p = api.Plan(m, kernel=api.KERNEL_L, arithmetic=api.ARITH_DF32)
+    assert p.info().arithmetic == api.ARITH_DF32
+    for bad in (1e30, 3e-20, 5e-324):
+        xv = G.vector(m.n_cols, seed=4)
+        xv[::97] = bad
+        check_f64(p.mxv_host(xv), m, xv)
+        xg = G.vector(m.n_cols, seed=5)
+        check_f64(p.mxv_host(xg), m, xg)
+    p.free()
+
+
+def test_df32_not_chosen_for_out_of_range_matrix(built):
+    from vnec_gb300 import api
+    from vnec_gb300 import generators as G
+
+    m = G.uniform_k(4000, 8, seed=1).copy()
+    m.val[5] = 1e-30
+    p = api.Plan(m, kernel=api.KERNEL_L)
+    assert p.info().arithmetic == api.ARITH_FP64
+    xv = G.vector(m.n_cols, seed=2)
+    check_f64(p.mxv_host(xv), m, xv)
+    p.free()
+    with pytest.raises(api.VnecError):
+        api.Plan(m, kernel=api.KERNEL_L, arithmetic=api.ARITH_DF32)
 
 
 def _custom(n_rows, n_cols, lens, seed=0):
@@ -148,8 +202,10 @@ def test_edge_cases(built, name):
         lens[[10, 2000, 3999]] = [30000, 45000, 29000]
         m = _custom(4000, 60000, lens, seed=6)
     xv = np.random.default_rng(2).uniform(-1, 1, size=m.n_cols)
-    for tpb, ipt in ((256, 7), (128, 4)):
-        p = api.Plan(m, kernel=api.KERNEL_L, threads_per_block=tpb, items_per_thread=ipt)
+    for kw in (dict(pipeline_stages=1), dict(pipeline_stages=1, threads_per_block=128, items_per_thread=4),
+               dict(arithmetic=api.ARITH_FP64), dict(arithmetic=api.ARITH_DF32),
+               dict(arithmetic=api.ARITH_DF32, threads_per_block=128, items_per_thread=12, pipeline_stages=3)):
+        p = api.Plan(m, kernel=api.KERNEL_L, **kw)
         y = p.mxv_host(xv)
         check_f64(y, m, xv)
         p.free()
@@ -187,17 +243,24 @@ def test_full_size_rmat_scale24(built):
 
     m = G.rmat(24, 1 << 28, seed=1)
     xv = G.vector(m.n_cols, seed=2)
-    p = api.Plan(m, kernel=api.KERNEL_L)
-    y = p.mxv_host(xv)
-    check_f64(y, m, xv)
-    y2 = p.mxv_host(xv)
-    assert y.tobytes() == y2.tobytes()
-    p.free()
-    kat, xk = G.kat_values(m)
-    rows = np.repeat(np.arange(m.n_rows, dtype=np.float64), np.diff(m.row_ptr))
-    exact = np.arange(m.n_rows, dtype=np.float64) * np.bincount(
-        rows.astype(np.int64), weights=m.col[: m.nnz].astype(np.float64), minlength=m.n_rows)
+    for kw in (dict(), dict(arithmetic=api.ARITH_FP64), dict(pipeline_stages=1)):
+        p = api.Plan(m, kernel=api.KERNEL_L, **kw)
+        y = p.mxv_host(xv)
+        check_f64(y, m, xv)
+        y2 = p.mxv_host(xv)
+        assert y.tobytes() == y2.tobytes()
+        p.free()
+    # Exact-integer pattern on the same structure (the harness's A_ij = i,
+    # x_j = j overflows 2^53 on this matrix): a_ij = (i mod 8) + 1 and
+    # x_j = j mod 4096 keep every partial sum an integer below 2^53, so the
+    # result is bit-exact in any summation order.
+    rows = np.repeat(np.arange(m.n_rows, dtype=np.int64), np.diff(m.row_ptr))
+    vals = (rows % 8 + 1).astype(np.float64)
+    xk = (np.arange(m.n_cols) % 4096).astype(np.float64)
+    exact = (np.arange(m.n_rows) % 8 + 1) * np.bincount(rows, weights=xk[m.col[: m.nnz]], minlength=m.n_rows)
     assert exact.max() < 2.0 ** 53
-    pk = api.Plan(kat, kernel=api.KERNEL_L)
-    assert pk.mxv_host(xk).tobytes() == exact.tobytes()
-    pk.free()
+    kat = G.from_arrays(m.n_rows, m.n_cols, m.row_ptr, m.col[: m.nnz], vals)
+    for ar in (api.ARITH_FP64, api.ARITH_DF32):
+        pk = api.Plan(kat, kernel=api.KERNEL_L, arithmetic=ar)
+        assert pk.mxv_host(xk).tobytes() == exact.astype(np.float64).tobytes()
+        pk.free()

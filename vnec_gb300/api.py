@@ -26,6 +26,7 @@ SpB_DENSE = 0
 SpB_CSC, SpB_CSR = 0, 1
 SpB_VNEC_D, SpB_VNEC_S = 0, 1
 KERNEL_AUTO, KERNEL_L, KERNEL_D, KERNEL_S = 0, 1, 2, 3
+ARITH_AUTO, ARITH_FP64, ARITH_DF32 = 0, 1, 2
 
 _DTYPE = {SpB_FP32: np.float32, SpB_FP64: np.float64}
 
@@ -58,7 +59,7 @@ class Options(C.Structure):
     """SpB_VNEC_options_ext."""
 
     _fields_ = [("kernel", C.c_int), ("threads_per_block", C.c_int), ("items_per_thread", C.c_int),
-                ("reserved", C.c_int * 13)]
+                ("pipeline_stages", C.c_int), ("arithmetic", C.c_int), ("reserved", C.c_int * 11)]
 
 
 class Info(C.Structure):
@@ -67,7 +68,8 @@ class Info(C.Structure):
     _fields_ = [("kernel", C.c_int), ("value_type", C.c_int), ("n_rows", C.c_int64), ("n_cols", C.c_int64),
                 ("nnz", C.c_int64), ("device_bytes", C.c_int64), ("algorithmic_bytes", C.c_int64),
                 ("launches_per_call", C.c_int), ("threads_per_block", C.c_int), ("items_per_thread", C.c_int),
-                ("num_tiles", C.c_int64), ("reserved", C.c_int * 8)]
+                ("num_tiles", C.c_int64), ("pipeline_stages", C.c_int), ("arithmetic", C.c_int),
+                ("reserved", C.c_int * 6)]
 
 
 _vp = C.c_void_p
@@ -109,6 +111,8 @@ def lib() -> C.CDLL:
     L.SpB_VNEC_set_profiling_ext.restype = C.c_int
     L.SpB_VNEC_kernel_ms_ext.argtypes = [_vp, C.POINTER(C.c_float), C.c_int]
     L.SpB_VNEC_kernel_ms_ext.restype = C.c_int
+    L.SpB_VNEC_device_status_ext.argtypes = [_vp, _vp]
+    L.SpB_VNEC_device_status_ext.restype = C.c_int
     L._vnec_typed = True
     return L
 
@@ -216,9 +220,11 @@ def SpB_mxv(y: Vector, A: Matrix, x: Vector, vnec: int | None = None) -> None:
 
 # --- extensions ---------------------------------------------------------------
 
-def options(kernel: int = KERNEL_AUTO, threads_per_block: int = 0, items_per_thread: int = 0) -> Options:
+def options(kernel: int = KERNEL_AUTO, threads_per_block: int = 0, items_per_thread: int = 0,
+            pipeline_stages: int = 0, arithmetic: int = ARITH_AUTO) -> Options:
     o = Options()
     o.kernel, o.threads_per_block, o.items_per_thread = kernel, threads_per_block, items_per_thread
+    o.pipeline_stages, o.arithmetic = pipeline_stages, arithmetic
     return o
 
 
@@ -259,6 +265,10 @@ class Plan:
             y = np.empty(inf_rows, dtype=self.dtype)
         _check(lib().SpB_mxv_host_ext(self.h, x.ctypes.data, y.ctypes.data) == SpB_SUCCESS, "SpB_mxv_host_ext")
         return y
+
+    def device_status(self, stream: int = 0) -> None:
+        """Raises VnecError if a bounded device wait of this plan timed out."""
+        _check(lib().SpB_VNEC_device_status_ext(self.h, stream or None) == SpB_SUCCESS, "device_status")
 
     def set_profiling(self, on: bool = True) -> None:
         _check(lib().SpB_VNEC_set_profiling_ext(self.h, int(on)) == SpB_SUCCESS, "set_profiling")

@@ -285,4 +285,14 @@ int SpB_VNEC_kernel_ms_ext(const void* plan, float* ms, int cap) {
   return p->kernel_ms(ms, cap);
 }
 
+SpB_Info SpB_VNEC_device_status_ext(void* plan, void* stream) {
+  clear_error();
+  Plan* p = find_plan(plan);
+  if (!p) {
+    set_error("unknown plan");
+    return SpB_FAILURE;
+  }
+  return p->device_status(static_cast<cudaStream_t>(stream)) ? SpB_SUCCESS : SpB_FAILURE;
+}
+
 }  // extern "C"

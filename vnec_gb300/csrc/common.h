@@ -79,4 +79,29 @@ size_t mp_smem_bytes(const MpShape& sh, size_t value_bytes);
 // Kernel launches per mp_spmv call.
 constexpr int kMpLaunchesPerCall = 2;
 
+// Pipelined merge-path kernels (mp2_kernels.cu): FP64 values, int32 offsets.
+struct Mp2Matrix {
+  int64_t n_rows = 0, n_cols = 0, nnz = 0;
+  const int* row_end = nullptr;  // padded by >= 4 elements
+  const int32_t* col = nullptr;  // padded by >= 4 elements
+  const double* val = nullptr;   // padded by >= 4 elements
+  const int* tile_row = nullptr;
+  const int* tile_nz = nullptr;
+  int* carry_row = nullptr;
+  double* carry_val = nullptr;
+  int* flags = nullptr;  // device [2]: DF32 range flag, pipeline timeout flag
+  int64_t num_tiles = 0;
+  MpShape shape;
+  int stages = 2;
+  int sms = 0;
+};
+// y = A x.  df32: double-float arithmetic on the FP32 pipe with an F64 guard
+// launch for out-of-range x.  Events as for mp_spmv.
+bool mp2_spmv(const Mp2Matrix& m, bool df32, const double* x, double* y, cudaStream_t s,
+              cudaEvent_t* events = nullptr);
+// Shared memory of a supported (threads, items, stages) combination, 0 if unsupported.
+size_t mp2_smem(int tpb, int ipt, int stages);
+// Kernel launches per mp2_spmv call.
+inline int mp2_launches(bool df32) { return df32 ? 3 : 2; }
+
 }  // namespace vnec

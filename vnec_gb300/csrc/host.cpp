@@ -198,7 +198,7 @@ bool Plan::run_host(const void* h_x, void* h_y) {
   if (!run(dx.ptr, dy.ptr, own_stream)) return false;
   if (n_rows > 0 && !VNEC_CUDA(cudaMemcpyAsync(h_y, dy.ptr, vb * n_rows, cudaMemcpyDeviceToHost, own_stream)))
     return false;
-  return VNEC_CUDA(cudaStreamSynchronize(own_stream));
+  return device_status(own_stream);
 }
 
 namespace {
@@ -235,13 +235,18 @@ std::unique_ptr<Plan> take_plan(const void* handle) {
 namespace {
 
 struct MergePathPlan final : Plan {
-  MpMatrix m;
-  DeviceBuffer row_end, col, val, tile_row, tile_nz, carry_row, carry_val;
+  MpMatrix m;     // unpipelined kernel (any value type / offset width)
+  Mp2Matrix m2;   // pipelined kernel (FP64, int32 offsets)
+  bool pipelined = false;
+  bool df32 = false;
+  DeviceBuffer row_end, col, val, tile_row, tile_nz, carry_row, carry_val, flags;
   MergePathPlan() : Plan(PlanKind::kMergePath) {}
   bool run(const void* d_x, void* d_y, cudaStream_t s) override {
     if (profiling && !ensure_events()) return false;
-    return mp_spmv(m, type == SpB_FP64 ? MpForm::kF64 : MpForm::kF32, d_x, d_y, s,
-                   profiling ? events : nullptr);
+    cudaEvent_t* ev = profiling ? events : nullptr;
+    if (pipelined)
+      return mp2_spmv(m2, df32, static_cast<const double*>(d_x), static_cast<double*>(d_y), s, ev);
+    return mp_spmv(m, type == SpB_FP64 ? MpForm::kF64 : MpForm::kF32, d_x, d_y, s, ev);
   }
   int kernel_ms(float* ms, int cap) const override {
     if (!profiling || !events[0] || cap < 2) return 0;
@@ -250,10 +255,13 @@ struct MergePathPlan final : Plan {
     cudaEventElapsedTime(&ms[1], events[1], events[2]);
     return 2;
   }
-  int launches_per_call() const override { return n_rows > 0 ? kMpLaunchesPerCall : 0; }
+  int launches_per_call() const override {
+    if (n_rows == 0) return 0;
+    return pipelined ? mp2_launches(df32) : kMpLaunchesPerCall;
+  }
   int64_t device_bytes() const override {
     return (int64_t)(row_end.bytes + col.bytes + val.bytes + tile_row.bytes + tile_nz.bytes + carry_row.bytes +
-                     carry_val.bytes + dx.bytes + dy.bytes);
+                     carry_val.bytes + flags.bytes + dx.bytes + dy.bytes);
   }
   int64_t algorithmic_bytes() const override {
     const int64_t vb = type == SpB_FP64 ? 8 : 4, ob = m.wide ? 8 : 4;
@@ -264,11 +272,43 @@ struct MergePathPlan final : Plan {
     info->threads_per_block = m.shape.tpb;
     info->items_per_thread = m.shape.ipt;
     info->num_tiles = m.num_tiles;
+    info->pipeline_stages = pipelined ? m2.stages : 0;
+    info->arithmetic = type == SpB_FP64 ? (df32 ? SpB_VNEC_ARITH_DF32 : SpB_VNEC_ARITH_FP64) : 0;
+  }
+  bool device_status(cudaStream_t s) override {
+    if (!pipelined) return VNEC_CUDA(cudaStreamSynchronize(s));
+    int h[2] = {0, 0};
+    if (!VNEC_CUDA(cudaMemcpyAsync(h, flags.ptr, sizeof(h), cudaMemcpyDeviceToHost, s))) return false;
+    if (!VNEC_CUDA(cudaStreamSynchronize(s))) return false;
+    if (h[1]) {
+      cudaMemsetAsync(flags.as<int>() + 1, 0, sizeof(int), s);
+      cudaStreamSynchronize(s);
+      set_error("merge-path pipeline: a bounded wait timed out (results of the affected call are invalid)");
+      return false;
+    }
+    return true;
   }
 };
 
 bool shape_supported(int tpb, int ipt) {
   return (tpb == 128 || tpb == 256) && (ipt == 4 || ipt == 7 || ipt == 10);
+}
+
+// DF32 splits every value into two floats; that needs |a| in [2^-40, 2^41)
+// (or a == 0) so that both halves and their products stay normal floats.
+bool values_df32_safe(const CsrView& v) {
+  if (v.type != SpB_FP64) return false;
+  const double* a = static_cast<const double*>(v.val);
+  int bad = 0;
+#pragma omp parallel for schedule(static) reduction(| : bad)
+  for (int64_t p = 0; p < v.nnz; ++p) {
+    uint64_t b;
+    std::memcpy(&b, a + p, 8);
+    const int e = (int)((b >> 52) & 0x7ff);
+    const bool zero = (b & 0x7FFFFFFFFFFFFFFFull) == 0;
+    if (!zero && (e - 1023 < -40 || e - 1023 > 40)) bad = 1;
+  }
+  return !bad;
 }
 
 }  // namespace
@@ -281,30 +321,48 @@ std::unique_ptr<Plan> build_merge_path(const CsrView& v, const SpB_VNEC_options_
   p->n_cols = v.n_cols;
   p->nnz = v.nnz;
   cudaGetDevice(&p->device);
+  const bool wide = (v.n_rows + v.nnz) >= ((int64_t)1 << 31) - 1;
+  const int req_stages = opts ? opts->pipeline_stages : 0;
+  const int req_arith = opts ? opts->arithmetic : SpB_VNEC_ARITH_AUTO;
+  // The pipelined kernel serves FP64 matrices with int32 merge coordinates.
+  p->pipelined = v.type == SpB_FP64 && !wide && req_stages != 1;
   MpShape sh;
+  if (p->pipelined) {
+    sh.tpb = 256;
+    sh.ipt = 7;
+  }
   if (opts && opts->threads_per_block) sh.tpb = opts->threads_per_block;
   if (opts && opts->items_per_thread) sh.ipt = opts->items_per_thread;
-  if (!shape_supported(sh.tpb, sh.ipt)) {
-    set_error("unsupported merge-path tile shape (threads 128/256, items 4/7/10)");
+  const int stages = req_stages >= 2 ? req_stages : 2;
+  if (p->pipelined ? mp2_smem(sh.tpb, sh.ipt, stages) == 0 : !shape_supported(sh.tpb, sh.ipt)) {
+    set_error(p->pipelined ? "unsupported pipelined tile shape (256x7 s2/s3, 256x12 s2, 128x12 s3, 512x5 s2)"
+                           : "unsupported merge-path tile shape (threads 128/256, items 4/7/10)");
     return nullptr;
+  }
+  if (p->pipelined) {
+    if (req_arith == SpB_VNEC_ARITH_DF32 && !values_df32_safe(v)) {
+      set_error("DF32 arithmetic requested but a matrix value lies outside [2^-40, 2^41)");
+      return nullptr;
+    }
+    p->df32 = req_arith == SpB_VNEC_ARITH_DF32 || (req_arith == SpB_VNEC_ARITH_AUTO && values_df32_safe(v));
   }
   MpMatrix& m = p->m;
   m.n_rows = v.n_rows;
   m.n_cols = v.n_cols;
   m.nnz = v.nnz;
   m.shape = sh;
-  m.wide = (v.n_rows + v.nnz) >= ((int64_t)1 << 31) - 1;
+  m.wide = wide;
   const size_t ob = m.wide ? 8 : 4;
   const size_t vb = v.value_bytes();
   const int64_t ipc = sh.items_per_tile();
   m.num_tiles = (v.n_rows + v.nnz + ipc - 1) / ipc;
-  // Device arrays are padded by 16 elements so that vector loads near the end
-  // stay inside the allocation.
+  // Device arrays are padded by 16 elements so that widened bulk copies and
+  // vector loads near the end stay inside the allocation.
   const size_t pad = 16;
   if (!p->row_end.alloc(ob * (v.n_rows + pad)) || !p->col.alloc(4 * (v.nnz + pad)) ||
       !p->val.alloc(vb * (v.nnz + pad)) || !p->tile_row.alloc(ob * (m.num_tiles + 1)) ||
       !p->tile_nz.alloc(ob * (m.num_tiles + 1)) || !p->carry_row.alloc(ob * (m.num_tiles + 1)) ||
-      !p->carry_val.alloc(vb * (m.num_tiles + 1)))
+      !p->carry_val.alloc(8 * (m.num_tiles + 1)) || !p->flags.alloc(64))
     return nullptr;
   {
     std::vector<unsigned char> host_end(ob * (size_t)std::max<int64_t>(v.n_rows, 1));
@@ -324,7 +382,9 @@ std::unique_ptr<Plan> build_merge_path(const CsrView& v, const SpB_VNEC_options_
   }
   // Zero the padding so no uninitialised value is ever read.
   if (!VNEC_CUDA(cudaMemset(p->col.as<char>() + 4 * v.nnz, 0, 4 * pad)) ||
-      !VNEC_CUDA(cudaMemset(p->val.as<char>() + vb * v.nnz, 0, vb * pad)))
+      !VNEC_CUDA(cudaMemset(p->val.as<char>() + vb * v.nnz, 0, vb * pad)) ||
+      !VNEC_CUDA(cudaMemset(p->row_end.as<char>() + ob * v.n_rows, 0, ob * pad)) ||
+      !VNEC_CUDA(cudaMemset(p->flags.ptr, 0, 64)))
     return nullptr;
   m.row_end = p->row_end.ptr;
   m.col = p->col.as<int32_t>();
@@ -333,6 +393,24 @@ std::unique_ptr<Plan> build_merge_path(const CsrView& v, const SpB_VNEC_options_
   m.tile_nz = p->tile_nz.ptr;
   m.carry_row = p->carry_row.ptr;
   m.carry_val = p->carry_val.ptr;
+  if (p->pipelined) {
+    Mp2Matrix& q = p->m2;
+    q.n_rows = v.n_rows;
+    q.n_cols = v.n_cols;
+    q.nnz = v.nnz;
+    q.row_end = p->row_end.as<int>();
+    q.col = p->col.as<int32_t>();
+    q.val = p->val.as<double>();
+    q.tile_row = p->tile_row.as<int>();
+    q.tile_nz = p->tile_nz.as<int>();
+    q.carry_row = p->carry_row.as<int>();
+    q.carry_val = p->carry_val.as<double>();
+    q.flags = p->flags.as<int>();
+    q.num_tiles = m.num_tiles;
+    q.shape = sh;
+    q.stages = stages;
+    if (!VNEC_CUDA(cudaDeviceGetAttribute(&q.sms, cudaDevAttrMultiProcessorCount, p->device))) return nullptr;
+  }
   if (v.n_rows > 0) {
     if (!mp_partition(m, nullptr)) return nullptr;
     if (!VNEC_CUDA(cudaDeviceSynchronize())) return nullptr;

@@ -65,6 +65,8 @@ struct Plan {
   virtual void describe(SpB_VNEC_info_ext* info) const = 0;
   // Milliseconds of each kernel of the last profiled call (main kernel first).
   virtual int kernel_ms(float* ms, int cap) const = 0;
+  // Waits for the plan's work on `s` and reports device-side errors.
+  virtual bool device_status(cudaStream_t s) { return VNEC_CUDA(cudaStreamSynchronize(s)); }
   bool run_host(const void* h_x, void* h_y);
 };
 
