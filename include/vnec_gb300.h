@@ -58,12 +58,26 @@ struct VNEC_L *Build_VNEC_L(const SpB_Matrix A);
 void SpMV_VNEC_L_FP32(SpB_Vector y, const SpB_Matrix A, const SpB_Vector x, VNEC_L *mat_thd);
 void SpMV_VNEC_L_FP64(SpB_Vector y, const SpB_Matrix A, const SpB_Vector x, VNEC_L *mat_thd);
 
+/* include/OpenSparseBLAS.h:2071 and :2012 (spmv_vnec_S_for_mxv.c:336-588,
+ * :3-334).  Sliced row-group plan: rows bucketed by length into interleaved
+ * groups of 32 lanes (the reference's equal-length cross-row groups, re-derived
+ * for warps), long rows split into chunks.  Pointer fields of the public
+ * struct are NULL.  Release with VNEC_S_free_fp64 / VNEC_S_free_fp32. */
+struct VNEC_S_FP64 *Build_VNEC_S_FP64(const SpB_Matrix A);
+struct VNEC_S_FP32 *Build_VNEC_S_FP32(const SpB_Matrix A);
+
+/* include/OpenSparseBLAS.h:2066 and :2007 (spmv_vnec_S_for_mxv.c:589-660, :255-334). */
+void SpMV_VNEC_S_FP64(SpB_Vector y, const SpB_Matrix A, const SpB_Vector x, VNEC_S_FP64 *mat_thd);
+void SpMV_VNEC_S_FP32(SpB_Vector y, const SpB_Matrix A, const SpB_Vector x, VNEC_S_FP32 *mat_thd);
+
 /* ------------------------------------------------------------------------ */
 /* Handle release (the reference frees handles field by field in its test    */
 /* code, src/operation/test/test_spmv_vnec.hpp:81-176 and                     */
 /* test_spmv_vnec.cpp:248-253; these library functions replace that).        */
 /* ------------------------------------------------------------------------ */
 void VNEC_L_free_ext(VNEC_L *mat_thd);
+void VNEC_S_free_fp64(VNEC_S_FP64 *mat_thd);
+void VNEC_S_free_fp32(VNEC_S_FP32 *mat_thd);
 
 /* ------------------------------------------------------------------------ */
 /* Extensions                                                                */
@@ -95,7 +109,10 @@ typedef struct {
   int items_per_thread;  /* 0: default */
   int pipeline_stages;   /* merge-path: 0 default (2), 1 unpipelined kernel, 2-3 stages */
   int arithmetic;        /* SpB_VNEC_arith_ext (FP64 values) */
-  int reserved[11];
+  int window_rows;       /* sliced: rows sorted within windows of this size (0: 65536) */
+  int long_row_len;      /* sliced: rows longer than this are chunked (0: 1024) */
+  int max_steps;         /* sliced: max 32-wide loads per lane for a row group (0: 32) */
+  int reserved[8];
 } SpB_VNEC_options_ext;
 
 /* Plan from raw host CSR arrays: int64 row offsets (n_rows + 1), int32

@@ -181,6 +181,18 @@ def _custom(n_rows, n_cols, lens, seed=0):
 def test_edge_cases(built, name):
     from vnec_gb300 import api
 
+    m = _edge_matrix(name)
+    xv = np.random.default_rng(2).uniform(-1, 1, size=m.n_cols)
+    for kw in (dict(pipeline_stages=1), dict(pipeline_stages=1, threads_per_block=128, items_per_thread=4),
+               dict(arithmetic=api.ARITH_FP64), dict(arithmetic=api.ARITH_DF32),
+               dict(arithmetic=api.ARITH_DF32, threads_per_block=128, items_per_thread=12, pipeline_stages=3)):
+        p = api.Plan(m, kernel=api.KERNEL_L, **kw)
+        y = p.mxv_host(xv)
+        check_f64(y, m, xv)
+        p.free()
+
+
+def _edge_matrix(name):
     if name == "empty_matrix":
         m = _custom(37, 41, np.zeros(37, dtype=int))
     elif name == "single_row_spanning_tiles":
@@ -201,14 +213,7 @@ def test_edge_cases(built, name):
         lens = np.where(rng.random(4000) < 0.5, 0, rng.integers(1, 20, size=4000))
         lens[[10, 2000, 3999]] = [30000, 45000, 29000]
         m = _custom(4000, 60000, lens, seed=6)
-    xv = np.random.default_rng(2).uniform(-1, 1, size=m.n_cols)
-    for kw in (dict(pipeline_stages=1), dict(pipeline_stages=1, threads_per_block=128, items_per_thread=4),
-               dict(arithmetic=api.ARITH_FP64), dict(arithmetic=api.ARITH_DF32),
-               dict(arithmetic=api.ARITH_DF32, threads_per_block=128, items_per_thread=12, pipeline_stages=3)):
-        p = api.Plan(m, kernel=api.KERNEL_L, **kw)
-        y = p.mxv_host(xv)
-        check_f64(y, m, xv)
-        p.free()
+    return m
 
 
 def test_device_pointers_on_torch_stream(built):
@@ -264,3 +269,79 @@ def test_full_size_rmat_scale24(built):
         pk = api.Plan(kat, kernel=api.KERNEL_L, arithmetic=ar)
         assert pk.mxv_host(xk).tobytes() == exact.astype(np.float64).tobytes()
         pk.free()
+
+
+# ---------------------------------------------------------------------------
+# Sliced row-group kernel (VNEC-S counterpart)
+# ---------------------------------------------------------------------------
+
+@pytest.mark.parametrize("case", golden_cases())
+@pytest.mark.parametrize("fp64", [True, False])
+def test_golden_sliced_dropin(built, case, fp64):
+    from vnec_gb300 import api
+
+    g = load_golden(case)
+    m = golden_csr(g)
+    dt = np.float64 if fp64 else np.float32
+    A = api.Matrix.from_csr(m, dtype=dt)
+    x = api.Vector(g["x"], dtype=dt)
+    y = api.Vector(np.full(m.n_rows, np.nan), dtype=dt)
+    if fp64:
+        h = api.Build_VNEC_S_FP64(A)
+        api.SpMV_VNEC_S_FP64(y, A, x, h)
+        api.VNEC_S_free_fp64(h)
+        if case.startswith("kat_"):
+            assert y.values.tobytes() == g["y_serial_f64"].tobytes()
+        else:
+            check_f64(y.values, m, g["x"])
+    else:
+        h = api.Build_VNEC_S_FP32(A)
+        api.SpMV_VNEC_S_FP32(y, A, x, h)
+        api.VNEC_S_free_fp32(h)
+        check_f32(y.values, m, g["x"])
+
+
+SLICED_PARAMS = [dict(), dict(window_rows=1000), dict(long_row_len=64), dict(max_steps=4),
+                 dict(window_rows=777, long_row_len=96, max_steps=8), dict(long_row_len=32, max_steps=1)]
+
+
+@pytest.mark.parametrize("kw", SLICED_PARAMS, ids=[str(k) for k in SLICED_PARAMS])
+def test_sliced_params(built, kw):
+    from vnec_gb300 import api
+    from vnec_gb300 import generators as G
+
+    for m in (G.rmat(16, 16 << 16, seed=7), G.lognormal(20000, sigma=2.5, cap=4096, seed=8),
+              G.stencil27(20, seed=9), G.banded(5000, 65, seed=3)):
+        xv = G.vector(m.n_cols, seed=9)
+        p = api.Plan(m, kernel=api.KERNEL_S, **kw)
+        y = p.mxv_host(xv)
+        check_f64(y, m, xv)
+        assert p.mxv_host(xv).tobytes() == y.tobytes()
+        p.free()
+
+
+@pytest.mark.parametrize("name", ["empty_matrix", "single_row_spanning_tiles", "all_rows_empty",
+                                  "single_entry", "rectangular_wide", "rectangular_tall", "tile_boundary",
+                                  "hub_rows_and_empties"])
+def test_sliced_edge_cases(built, name):
+    from vnec_gb300 import api
+
+    m = _edge_matrix(name)
+    xv = np.random.default_rng(2).uniform(-1, 1, size=m.n_cols)
+    for kw in (dict(), dict(long_row_len=40, window_rows=100)):
+        p = api.Plan(m, kernel=api.KERNEL_S, **kw)
+        check_f64(p.mxv_host(xv), m, xv)
+        p.free()
+
+
+def test_sliced_full_size_rmat_scale24(built):
+    from vnec_gb300 import api
+    from vnec_gb300 import generators as G
+
+    m = G.rmat(24, 1 << 28, seed=1)
+    xv = G.vector(m.n_cols, seed=2)
+    p = api.Plan(m, kernel=api.KERNEL_S)
+    y = p.mxv_host(xv)
+    check_f64(y, m, xv)
+    assert p.mxv_host(xv).tobytes() == y.tobytes()
+    p.free()

@@ -59,7 +59,8 @@ class Options(C.Structure):
     """SpB_VNEC_options_ext."""
 
     _fields_ = [("kernel", C.c_int), ("threads_per_block", C.c_int), ("items_per_thread", C.c_int),
-                ("pipeline_stages", C.c_int), ("arithmetic", C.c_int), ("reserved", C.c_int * 11)]
+                ("pipeline_stages", C.c_int), ("arithmetic", C.c_int), ("window_rows", C.c_int),
+                ("long_row_len", C.c_int), ("max_steps", C.c_int), ("reserved", C.c_int * 8)]
 
 
 class Info(C.Structure):
@@ -86,11 +87,15 @@ def lib() -> C.CDLL:
     L.IRD_VNEC.restype = C.c_int
     L.Build_VNEC_L.argtypes = [_vp]
     L.Build_VNEC_L.restype = _vp
-    for f in ("SpMV_VNEC_L_FP64", "SpMV_VNEC_L_FP32"):
+    for f in ("SpMV_VNEC_L_FP64", "SpMV_VNEC_L_FP32", "SpMV_VNEC_S_FP64", "SpMV_VNEC_S_FP32"):
         getattr(L, f).argtypes = [_vp, _vp, _vp, _vp]
         getattr(L, f).restype = None
-    L.VNEC_L_free_ext.argtypes = [_vp]
-    L.VNEC_L_free_ext.restype = None
+    for f in ("Build_VNEC_S_FP64", "Build_VNEC_S_FP32"):
+        getattr(L, f).argtypes = [_vp]
+        getattr(L, f).restype = _vp
+    for f in ("VNEC_L_free_ext", "VNEC_S_free_fp64", "VNEC_S_free_fp32"):
+        getattr(L, f).argtypes = [_vp]
+        getattr(L, f).restype = None
     L.SpB_VNEC_last_error_ext.argtypes = []
     L.SpB_VNEC_last_error_ext.restype = C.c_char_p
     L.SpB_VNEC_plan_ext.argtypes = [C.POINTER(Options), C.c_int, C.c_int64, C.c_int64, _vp, _vp, _vp]
@@ -214,6 +219,36 @@ def VNEC_L_free(h: int) -> None:
     lib().VNEC_L_free_ext(h)
 
 
+def Build_VNEC_S_FP64(A: Matrix) -> int:
+    h = lib().Build_VNEC_S_FP64(A.handle)
+    _check(bool(h), "Build_VNEC_S_FP64")
+    return h
+
+
+def Build_VNEC_S_FP32(A: Matrix) -> int:
+    h = lib().Build_VNEC_S_FP32(A.handle)
+    _check(bool(h), "Build_VNEC_S_FP32")
+    return h
+
+
+def SpMV_VNEC_S_FP64(y: Vector, A: Matrix, x: Vector, h: int) -> None:
+    lib().SpMV_VNEC_S_FP64(y.handle, A.handle, x.handle, h)
+    _check(last_error() == "", "SpMV_VNEC_S_FP64")
+
+
+def SpMV_VNEC_S_FP32(y: Vector, A: Matrix, x: Vector, h: int) -> None:
+    lib().SpMV_VNEC_S_FP32(y.handle, A.handle, x.handle, h)
+    _check(last_error() == "", "SpMV_VNEC_S_FP32")
+
+
+def VNEC_S_free_fp64(h: int) -> None:
+    lib().VNEC_S_free_fp64(h)
+
+
+def VNEC_S_free_fp32(h: int) -> None:
+    lib().VNEC_S_free_fp32(h)
+
+
 def SpB_mxv(y: Vector, A: Matrix, x: Vector, vnec: int | None = None) -> None:
     _check(lib().SpB_mxv(y.handle, A.handle, x.handle, vnec) == SpB_SUCCESS, "SpB_mxv")
 
@@ -221,10 +256,12 @@ def SpB_mxv(y: Vector, A: Matrix, x: Vector, vnec: int | None = None) -> None:
 # --- extensions ---------------------------------------------------------------
 
 def options(kernel: int = KERNEL_AUTO, threads_per_block: int = 0, items_per_thread: int = 0,
-            pipeline_stages: int = 0, arithmetic: int = ARITH_AUTO) -> Options:
+            pipeline_stages: int = 0, arithmetic: int = ARITH_AUTO, window_rows: int = 0, long_row_len: int = 0,
+            max_steps: int = 0) -> Options:
     o = Options()
     o.kernel, o.threads_per_block, o.items_per_thread = kernel, threads_per_block, items_per_thread
     o.pipeline_stages, o.arithmetic = pipeline_stages, arithmetic
+    o.window_rows, o.long_row_len, o.max_steps = window_rows, long_row_len, max_steps
     return o
 
 

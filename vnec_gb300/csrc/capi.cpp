@@ -4,6 +4,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <mutex>
+#include <type_traits>
 #include <unordered_map>
 
 #include "host.h"
@@ -26,6 +27,46 @@ Pub* publish(std::unique_ptr<Plan> plan) {
   }
   register_plan(pub, std::move(plan));
   return pub;
+}
+
+// The reference harness releases D/S handles field by field and indexes the
+// per-partition pointer arrays up to NUM_THREADS (36 or 48) before freeing
+// them (test_spmv_vnec.hpp:130-176).  Those arrays are therefore allocated as
+// NULL-filled blocks of kPartSlots entries, so that pattern stays memory-safe.
+constexpr int kPartSlots = 64;
+
+template <typename Pub>
+void fill_part_arrays(Pub* pub) {
+  pub->use_x_indices = static_cast<int**>(std::calloc(kPartSlots, sizeof(int*)));
+  using XV = std::remove_pointer_t<decltype(pub->ecr_xx_val)>;
+  pub->ecr_xx_val = static_cast<decltype(pub->ecr_xx_val)>(std::calloc(kPartSlots, sizeof(XV)));
+}
+
+template <typename Pub>
+void free_part_arrays(Pub* pub) {
+  std::free(pub->use_x_indices);
+  std::free(pub->ecr_xx_val);
+}
+
+template <typename Pub>
+Pub* publish_s(std::unique_ptr<Plan> plan) {
+  if (plan) plan->pub_part_arrays = true;
+  Pub* pub = publish<Pub>(std::move(plan));
+  if (pub) {
+    fill_part_arrays(pub);
+    pub->tasks = static_cast<int**>(std::calloc(kPartSlots, sizeof(int*)));
+  }
+  return pub;
+}
+
+template <typename Pub>
+void free_s(Pub* pub) {
+  if (!pub) return;
+  std::unique_ptr<Plan> p = take_plan(pub);
+  if (!p) return;
+  free_part_arrays(pub);
+  std::free(pub->tasks);
+  std::free(pub);
 }
 
 bool host_vector(const SpB_Vector v, SpB_Type type, int64_t n, void** values) {
@@ -82,6 +123,8 @@ std::unique_ptr<Plan> build_from_view(const CsrView& v, const SpB_VNEC_options_e
     case SpB_VNEC_KERNEL_AUTO:
     case SpB_VNEC_KERNEL_L:
       return build_merge_path(v, opts);
+    case SpB_VNEC_KERNEL_S:
+      return build_sliced(v, opts);
     default:
       set_error("requested kernel is not available");
       return nullptr;
@@ -189,6 +232,60 @@ void SpMV_VNEC_L_FP32(SpB_Vector y, const SpB_Matrix A, const SpB_Vector x, VNEC
 
 void VNEC_L_free_ext(VNEC_L* mat_thd) { SpB_VNEC_plan_free_ext(mat_thd); }
 
+static Plan* typed_plan(const void* h, SpB_Type t, PlanKind k, const char* fn) {
+  Plan* p = find_plan(h);
+  if (!p) {
+    set_error(std::string(fn) + ": unknown handle");
+    return nullptr;
+  }
+  if (p->kind != k) {
+    set_error(std::string(fn) + ": handle was built for another VNEC variant");
+    return nullptr;
+  }
+  if (p->type != t) {
+    set_error(std::string(fn) + ": handle value type does not match");
+    return nullptr;
+  }
+  return p;
+}
+
+struct VNEC_S_FP64* Build_VNEC_S_FP64(const SpB_Matrix A) {
+  clear_error();
+  CsrView v;
+  if (!view_from_matrix(A, &v)) return nullptr;
+  if (v.type != SpB_FP64) {
+    set_error("Build_VNEC_S_FP64: matrix is not FP64");
+    return nullptr;
+  }
+  return publish_s<VNEC_S_FP64>(build_sliced(v, nullptr));
+}
+
+struct VNEC_S_FP32* Build_VNEC_S_FP32(const SpB_Matrix A) {
+  clear_error();
+  CsrView v;
+  if (!view_from_matrix(A, &v)) return nullptr;
+  if (v.type != SpB_FP32) {
+    set_error("Build_VNEC_S_FP32: matrix is not FP32");
+    return nullptr;
+  }
+  return publish_s<VNEC_S_FP32>(build_sliced(v, nullptr));
+}
+
+void SpMV_VNEC_S_FP64(SpB_Vector y, const SpB_Matrix A, const SpB_Vector x, VNEC_S_FP64* mat_thd) {
+  clear_error();
+  Plan* p = typed_plan(mat_thd, SpB_FP64, PlanKind::kWindowSliced, "SpMV_VNEC_S_FP64");
+  if (p) run_mxv(y, A, x, p);
+}
+
+void SpMV_VNEC_S_FP32(SpB_Vector y, const SpB_Matrix A, const SpB_Vector x, VNEC_S_FP32* mat_thd) {
+  clear_error();
+  Plan* p = typed_plan(mat_thd, SpB_FP32, PlanKind::kWindowSliced, "SpMV_VNEC_S_FP32");
+  if (p) run_mxv(y, A, x, p);
+}
+
+void VNEC_S_free_fp64(VNEC_S_FP64* mat_thd) { free_s(mat_thd); }
+void VNEC_S_free_fp32(VNEC_S_FP32* mat_thd) { free_s(mat_thd); }
+
 const char* SpB_VNEC_last_error_ext(void) { return last_error(); }
 
 void* SpB_VNEC_plan_ext(const SpB_VNEC_options_ext* opts, SpB_Type type, int64_t n_rows, int64_t n_cols,
@@ -212,8 +309,17 @@ void* SpB_VNEC_plan_matrix_ext(const SpB_VNEC_options_ext* opts, const SpB_Matri
 
 void SpB_VNEC_plan_free_ext(void* plan) {
   if (!plan) return;
-  std::unique_ptr<Plan> p = take_plan(plan);
-  if (p) std::free(plan);
+  Plan* p = find_plan(plan);
+  if (!p) return;
+  if (p->pub_part_arrays && p->kind == PlanKind::kWindowSliced) {
+    if (p->type == SpB_FP64)
+      free_s(static_cast<VNEC_S_FP64*>(plan));
+    else
+      free_s(static_cast<VNEC_S_FP32*>(plan));
+    return;
+  }
+  take_plan(plan);
+  std::free(plan);
 }
 
 void SpB_VNEC_forget_ext(const SpB_Matrix A) {

@@ -50,6 +50,9 @@ struct Plan {
   int device = 0;
   cudaStream_t own_stream = nullptr;
   DeviceBuffer dx, dy;  // staging for host-vector calls
+  // The public handle carries NULL-filled per-partition pointer arrays
+  // (Build_VNEC_S_* / Build_VNEC_D_*) that the release must free.
+  bool pub_part_arrays = false;
   // Per-kernel timing of the most recent call (SpB_VNEC_set_profiling_ext).
   bool profiling = false;
   cudaEvent_t events[4] = {nullptr, nullptr, nullptr, nullptr};
@@ -77,6 +80,7 @@ std::unique_ptr<Plan> take_plan(const void* handle);
 
 // Plan builders.
 std::unique_ptr<Plan> build_merge_path(const CsrView& v, const SpB_VNEC_options_ext* opts);
+std::unique_ptr<Plan> build_sliced(const CsrView& v, const SpB_VNEC_options_ext* opts);
 
 // Reference partition count and lane width constants used by IRD_VNEC.
 struct IrdParams {

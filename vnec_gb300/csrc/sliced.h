@@ -1,0 +1,68 @@
+// Sliced row-group format (VNEC-S counterpart) shared by the host builder
+// (sliced_build.cpp) and the kernels (sliced_kernels.cu).
+#pragma once
+
+#include <cstdint>
+
+#include <cuda_runtime.h>
+
+namespace vnec {
+
+// One warp task = one 16-byte descriptor.
+//   kind ROWS : G = 32 >> vw_log2 rows of one group, each padded to `steps * VW`
+//               entries; entry j of group row g sits at
+//               base + (j / VW) * 32 + g * VW + (j % VW).  y[rowid[row_base+g]] = sum.
+//   kind CHUNK: a 32*steps-entry piece of a long row (VW = 32, G = 1); the sum
+//               goes to chunk_sum[row_base] and a fix-up adds the pieces.
+//   kind ZERO : `nrows` empty rows, y[rowid[row_base + lane]] = 0.
+enum SlicedKind : int { kSlicedRows = 0, kSlicedChunk = 1, kSlicedZero = 2 };
+
+struct SlicedTask {
+  int32_t base;      // first entry (element index into vals / cols)
+  int32_t row_base;  // index into rowid (ROWS, ZERO) or chunk id (CHUNK)
+  int32_t steps;     // warp-wide load steps (32 entries each)
+  int32_t meta;      // kind | vw_log2 << 4 | nrows << 8
+};
+
+struct SlicedMatrix {
+  int64_t n_rows = 0, n_cols = 0, nnz = 0, entries = 0;  // entries include padding
+  int64_t num_tasks = 0, num_long = 0, num_chunks = 0;
+  const SlicedTask* tasks = nullptr;
+  const void* val = nullptr;        // entries (double or float), padding = 0
+  const int32_t* col = nullptr;     // entries, padding = a valid column
+  const int32_t* rowid = nullptr;   // group row slots
+  const int32_t* long_row = nullptr;    // num_long rows
+  const int32_t* long_first = nullptr;  // num_long + 1 chunk offsets
+  void* chunk_sum = nullptr;            // num_chunks scratch (value type)
+};
+
+struct SlicedParams {
+  int window_rows = 1 << 16;  // rows sorted / grouped within windows of this size
+  int long_len = 1024;        // rows longer than this are split into chunks
+  int chunk = 1024;           // entries per chunk (multiple of 32)
+  int max_steps = 32;         // target load steps per lane for grouped rows
+};
+
+// Host-side arrays of a built sliced matrix.
+struct SlicedHost;
+SlicedHost* sliced_build(int64_t n_rows, int64_t n_cols, const int64_t* row_ptr_or_null,
+                         const uint64_t* row_ptr64_or_null, const int32_t* col_or_null,
+                         const uint64_t* col64_or_null, const void* val, int value_bytes, const SlicedParams& prm);
+void sliced_free(SlicedHost* h);
+// Uploads a built matrix; device buffers are owned by the caller-provided allocator.
+struct SlicedHostView {
+  int64_t entries, num_tasks, num_long, num_chunks, n_rowid;
+  const SlicedTask* tasks;
+  const void* val;
+  const int32_t* col;
+  const int32_t* rowid;
+  const int32_t* long_row;
+  const int32_t* long_first;
+};
+SlicedHostView sliced_view(const SlicedHost* h);
+
+bool sliced_spmv(const SlicedMatrix& m, bool fp64, const void* x, void* y, cudaStream_t s,
+                 cudaEvent_t* events = nullptr);
+inline int sliced_launches(const SlicedMatrix& m) { return m.num_long > 0 ? 2 : 1; }
+
+}  // namespace vnec
