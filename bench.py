@@ -211,7 +211,8 @@ def run_ours(args) -> None:
     t_gen = time.time() - t_gen
     B = algorithmic_bytes(m)
     t_plan = time.time()
-    plan = api.Plan(m, kernel=api.KERNEL_L)
+    kernel = {"L": api.KERNEL_L, "S": api.KERNEL_S}[args.kernel]
+    plan = api.Plan(m, kernel=kernel)
     t_plan = time.time() - t_plan
     info = plan.info()
     stream = torch.cuda.Stream(device=dev)
@@ -291,7 +292,7 @@ def run_ours(args) -> None:
     rel = O.rowwise_error(y_dev, y_ref, cond)
 
     peak, peak_src = measured_peaks()
-    kname = "mp_spmv_f64"
+    kname = {"L": "mp2_kernel", "S": "sliced_kernel"}[args.kernel]
     achieved = B / (np.mean(main_ms) / 1e3) / 1e9
     traffic = profiled_traffic(kname, args.workload)
     line = {
@@ -300,7 +301,10 @@ def run_ours(args) -> None:
         "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded generator, resident in HBM before timing)",
         "config": {"workload": desc, "n_rows": m.n_rows, "n_cols": m.n_cols, "nnz": m.nnz,
-                   "algorithmic_bytes": B, "kernel": "merge-path CSR FP64 (VNEC-L counterpart)",
+                   "algorithmic_bytes": B,
+                   "kernel": {"L": "merge-path CSR (VNEC-L counterpart)",
+                              "S": "sliced row groups (VNEC-S counterpart)"}[args.kernel],
+                   "arithmetic": "fp64 fma" if info.arithmetic != 2 else "df32 (double-float on FP32 pipe)",
                    "tile": f"{info.threads_per_block}x{info.items_per_thread}", "tiles": info.num_tiles,
                    "l2": "flushed before every timed step (512 MiB device write, outside the events)",
                    "parallelism": "replicas" if ws > 1 else "single GPU",
@@ -336,6 +340,7 @@ def main() -> None:
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", default="rmat24", choices=["rmat24", "rmat22", "uniform64k", "stencil256"])
+    ap.add_argument("--kernel", default="S", choices=["L", "S"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-budget", type=float, default=20.0, help="seconds of CPU-baseline timing")
     args = ap.parse_args()
