@@ -112,7 +112,8 @@ typedef struct {
   int window_rows;       /* sliced: rows sorted within windows of this size (0: 65536) */
   int long_row_len;      /* sliced: rows longer than this are chunked (0: 1024) */
   int max_steps;         /* sliced: max 32-wide loads per lane for a row group (0: 32) */
-  int reserved[8];
+  int cache_hints;       /* sliced: 0 default (streaming loads), 2 explicit L1/L2 evict policies */
+  int reserved[7];
 } SpB_VNEC_options_ext;
 
 /* Plan from raw host CSR arrays: int64 row offsets (n_rows + 1), int32

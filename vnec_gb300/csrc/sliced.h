@@ -34,6 +34,7 @@ struct SlicedMatrix {
   const int32_t* long_row = nullptr;    // num_long rows
   const int32_t* long_first = nullptr;  // num_long + 1 chunk offsets
   void* chunk_sum = nullptr;            // num_chunks scratch (value type)
+  int cache_hints = 0;                  // 0: streaming/read-only defaults, 1: explicit L1/L2 policies
 };
 
 struct SlicedParams {

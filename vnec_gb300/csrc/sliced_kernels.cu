@@ -6,8 +6,9 @@
 // of group row l / VW; a VW-lane xor-shuffle reduction finishes each row
 // (VW = 1: the reference's cross-row kernel, one lane per row, no reduction).
 // CHUNK tasks do the same for 32-wide pieces of long rows and a second launch
-// adds the pieces of each long row in chunk order.  Loads of values and
-// columns are streamed (read once); x is gathered through the read-only path.
+// adds the pieces of each long row in chunk order.  Values and columns are
+// read once (no L1 allocation, L2 evict-first policy); x is gathered through
+// the read-only path with evict-last policies.
 // FP64 work: one FMA per entry plus log2(VW) adds per row.
 
 #include <cuda_runtime.h>
@@ -23,11 +24,56 @@ namespace {
 constexpr unsigned kFull = 0xffffffffu;
 constexpr int kWarpsPerBlock = 8;
 
+// Loads with explicit cache policies (hint 1): values and columns are read
+// once — no L1 allocation, L2 policy evict_first — while x is kept (L1
+// evict_last, L2 policy evict_last) so its hot part stays cached across tasks.
+struct Policies {
+  unsigned long long once, keep;
+};
+__device__ __forceinline__ Policies make_policies() {
+  Policies p;
+  asm("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p.once));
+  asm("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p.keep));
+  return p;
+}
+__device__ __forceinline__ double ld_once(const double* p, unsigned long long pol) {
+  double v;
+  asm("ld.global.nc.L1::no_allocate.L2::cache_hint.f64 %0, [%1], %2;" : "=d"(v) : "l"(p), "l"(pol));
+  return v;
+}
+__device__ __forceinline__ float ld_once(const float* p, unsigned long long pol) {
+  float v;
+  asm("ld.global.nc.L1::no_allocate.L2::cache_hint.f32 %0, [%1], %2;" : "=f"(v) : "l"(p), "l"(pol));
+  return v;
+}
+__device__ __forceinline__ int ld_once(const int* p, unsigned long long pol) {
+  int v;
+  asm("ld.global.nc.L1::no_allocate.L2::cache_hint.s32 %0, [%1], %2;" : "=r"(v) : "l"(p), "l"(pol));
+  return v;
+}
+__device__ __forceinline__ double ld_keep(const double* p, unsigned long long pol) {
+  double v;
+  asm("ld.global.nc.L1::evict_last.L2::cache_hint.f64 %0, [%1], %2;" : "=d"(v) : "l"(p), "l"(pol));
+  return v;
+}
+__device__ __forceinline__ float ld_keep(const float* p, unsigned long long pol) {
+  float v;
+  asm("ld.global.nc.L1::evict_last.L2::cache_hint.f32 %0, [%1], %2;" : "=f"(v) : "l"(p), "l"(pol));
+  return v;
+}
+
+template <int H, typename T> __device__ __forceinline__ T ld_stream_h(const T* p, const Policies& pol) {
+  if constexpr (H == 0) return __ldcs(p); else return ld_once(p, pol.once);
+}
+template <int H, typename T> __device__ __forceinline__ T ld_x_h(const T* p, const Policies& pol) {
+  if constexpr (H == 0) return __ldg(p); else return ld_keep(p, pol.keep);
+}
+
 template <typename V> __device__ __forceinline__ V fmav(V a, V b, V c);
 template <> __device__ __forceinline__ double fmav<double>(double a, double b, double c) { return fma(a, b, c); }
 template <> __device__ __forceinline__ float fmav<float>(float a, float b, float c) { return fmaf(a, b, c); }
 
-template <typename V, int U>
+template <typename V, int U, int H>
 __global__ void __launch_bounds__(kWarpsPerBlock * 32)
 sliced_kernel(const SlicedTask* __restrict__ tasks, long long num_tasks, const V* __restrict__ val,
               const int32_t* __restrict__ col, const int32_t* __restrict__ rowid, const V* __restrict__ x,
@@ -44,6 +90,7 @@ sliced_kernel(const SlicedTask* __restrict__ tasks, long long num_tasks, const V
   }
   const V* vp = val + base + lane;
   const int32_t* cp = col + base + lane;
+  const Policies pol = make_policies();
   V acc = V(0);
   int k = 0;
   for (; k + U <= steps; k += U) {
@@ -51,15 +98,16 @@ sliced_kernel(const SlicedTask* __restrict__ tasks, long long num_tasks, const V
     V v[U], xv[U];
 #pragma unroll
     for (int u = 0; u < U; ++u) {
-      c[u] = __ldcs(cp + (k + u) * 32);
-      v[u] = __ldcs(vp + (k + u) * 32);
+      c[u] = ld_stream_h<H>(cp + (k + u) * 32, pol);
+      v[u] = ld_stream_h<H>(vp + (k + u) * 32, pol);
     }
 #pragma unroll
-    for (int u = 0; u < U; ++u) xv[u] = __ldg(x + c[u]);
+    for (int u = 0; u < U; ++u) xv[u] = ld_x_h<H>(x + c[u], pol);
 #pragma unroll
     for (int u = 0; u < U; ++u) acc = fmav<V>(v[u], xv[u], acc);
   }
-  for (; k < steps; ++k) acc = fmav<V>(__ldcs(vp + k * 32), __ldg(x + __ldcs(cp + k * 32)), acc);
+  for (; k < steps; ++k)
+    acc = fmav<V>(ld_stream_h<H>(vp + k * 32, pol), ld_x_h<H>(x + ld_stream_h<H>(cp + k * 32, pol), pol), acc);
   for (int off = (1 << vwl) >> 1; off > 0; off >>= 1) acc += __shfl_xor_sync(kFull, acc, off);
   if (kind == kSlicedChunk) {
     if (lane == 0) chunk_sum[row_base] = acc;
@@ -79,19 +127,32 @@ __global__ void sliced_long_fixup(const int32_t* __restrict__ long_row, const in
   y[long_row[i]] = s;
 }
 
+template <typename V, int H>
+bool launch_main(const SlicedMatrix& m, const void* x, void* y, cudaStream_t s) {
+  auto kern = sliced_kernel<V, 8, H>;
+  static bool configured = false;
+  if (!configured) {
+    // No shared memory: give the whole unified L1/shared array to L1.
+    if (!VNEC_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 0))) return false;
+    configured = true;
+  }
+  const long long grid = (m.num_tasks + kWarpsPerBlock - 1) / kWarpsPerBlock;
+  if (grid > 0x7fffffffLL) {
+    set_error("sliced: too many tasks for one launch");
+    return false;
+  }
+  kern<<<(unsigned)grid, kWarpsPerBlock * 32, 0, s>>>(m.tasks, m.num_tasks, static_cast<const V*>(m.val), m.col,
+                                                      m.rowid, static_cast<const V*>(x), static_cast<V*>(y),
+                                                      static_cast<V*>(m.chunk_sum));
+  return VNEC_CUDA(cudaGetLastError());
+}
+
 template <typename V>
 bool launch(const SlicedMatrix& m, const void* x, void* y, cudaStream_t s, cudaEvent_t* ev) {
   if (ev && !VNEC_CUDA(cudaEventRecord(ev[0], s))) return false;
   if (m.num_tasks > 0) {
-    const long long grid = (m.num_tasks + kWarpsPerBlock - 1) / kWarpsPerBlock;
-    if (grid > 0x7fffffffLL) {
-      set_error("sliced: too many tasks for one launch");
-      return false;
-    }
-    sliced_kernel<V, 8><<<(unsigned)grid, kWarpsPerBlock * 32, 0, s>>>(
-        m.tasks, m.num_tasks, static_cast<const V*>(m.val), m.col, m.rowid, static_cast<const V*>(x),
-        static_cast<V*>(y), static_cast<V*>(m.chunk_sum));
-    if (!VNEC_CUDA(cudaGetLastError())) return false;
+    const bool ok = m.cache_hints ? launch_main<V, 1>(m, x, y, s) : launch_main<V, 0>(m, x, y, s);
+    if (!ok) return false;
   }
   if (ev && !VNEC_CUDA(cudaEventRecord(ev[1], s))) return false;
   if (m.num_long > 0) {

@@ -93,6 +93,7 @@ std::unique_ptr<Plan> build_sliced(const CsrView& v, const SpB_VNEC_options_ext*
   m.long_row = p->long_row.as<int32_t>();
   m.long_first = p->long_first.as<int32_t>();
   m.chunk_sum = p->chunk_sum.ptr;
+  m.cache_hints = (opts && opts->cache_hints == 2) ? 1 : 0;
   return p;
 }
 
