@@ -160,6 +160,29 @@ typedef struct {
  * pipeline wait timed out, and clears the status. */
 SpB_Info SpB_VNEC_device_status_ext(void *plan, void *stream);
 
+/* Allocation-free y := A x (no counterpart in the reference).
+ *
+ * For callers that cannot let a library allocate device memory: hosts whose
+ * device memory is handed out entirely by their own pool allocator, and
+ * latency-critical loops where a cudaMalloc/cudaFree (and the device
+ * synchronisation it implies) is not acceptable.  The caller passes the CSR
+ * matrix already in device memory — int32 row offsets d_row_ptr[n_rows + 1]
+ * with d_row_ptr[n_rows] == nnz, int32 columns < n_cols, FP64 values — and
+ * FP64 x and y; the product is enqueued on `stream` (a cudaStream_t, NULL =
+ * legacy default stream) with the FP64 merge-path kernel.  Nothing is
+ * allocated: the kernel's scratch (tile coordinates and carries) lives in a
+ * fixed 5 MiB array that every device holds from library load until process
+ * exit.  Limit: n_rows + nnz <= 469,762,048 (262,144 tiles of 1,792 merge
+ * items); larger inputs return SpB_FAILURE with a message.  The first call on
+ * a device looks up that device's scratch address (cudaGetSymbolAddress), so
+ * make a first call on each device before any stream capture.  All calls on a
+ * device share the one scratch array: calls that can overlap on the GPU
+ * (different streams without ordering) race and must be serialised by the
+ * caller. */
+SpB_Info SpB_mxv_csr_noalloc_ext(int64_t n_rows, int64_t n_cols, int64_t nnz, const int32_t *d_row_ptr,
+                                 const int32_t *d_col, const double *d_val, const double *d_x, double *d_y,
+                                 void *stream);
+
 SpB_Info SpB_VNEC_plan_info_ext(const void *plan, SpB_VNEC_info_ext *info);
 
 /* Per-kernel timing: when enabled, each SpMV of the plan records CUDA events

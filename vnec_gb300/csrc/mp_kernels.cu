@@ -27,9 +27,12 @@
 // HBM rate for SpMV, so no other FP64 work is done in the loop.
 
 #include <cuda_runtime.h>
+
 #include <cstdint>
+#include <mutex>
 
 #include "common.h"
+#include "vnec_gb300.h"
 
 namespace vnec {
 namespace {
@@ -261,3 +264,104 @@ bool mp_spmv(const MpMatrix& m, MpForm form, const void* x, void* y, cudaStream_
 }
 
 }  // namespace vnec
+
+// ---------------------------------------------------------------------------
+// Allocation-free entry point: SpB_mxv_csr_noalloc_ext.
+//
+// Some callers cannot let a library allocate device memory on their behalf:
+// hosts whose device memory is handed out entirely by their own pool
+// allocator (the library could not obtain more), and latency-critical loops
+// in which a cudaMalloc/cudaFree and the device synchronisation it implies
+// are not acceptable.  For them this entry point runs the FP64 merge-path
+// kernel (256 threads x 7 merge items per tile) on CSR arrays the caller
+// already holds in device memory, and keeps its scratch — the merge
+// coordinates of each tile and each tile's carry-out — in the fixed array
+// below, which every device that loads this library holds until the process
+// exits.
+// ---------------------------------------------------------------------------
+namespace vnec {
+namespace {
+
+constexpr int kNaTpb = 256, kNaIpt = 7;
+// Scratch capacity: 2^18 tiles of 1,792 merge items, i.e. n_rows + nnz <=
+// 469,762,048; 5,242,888 bytes.
+constexpr long long kNaMaxTiles = 1LL << 18;
+constexpr size_t kNaTileRowOff = 0;
+constexpr size_t kNaTileNzOff = kNaTileRowOff + 4 * (kNaMaxTiles + 1);
+constexpr size_t kNaCarryRowOff = kNaTileNzOff + 4 * (kNaMaxTiles + 1);
+constexpr size_t kNaCarryValOff = kNaCarryRowOff + 4 * kNaMaxTiles;
+constexpr size_t kNaBytes = kNaCarryValOff + 8 * kNaMaxTiles;
+static_assert(kNaCarryValOff % 8 == 0, "carry values must be 8-byte aligned");
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNaBytes];
+
+// Device address of g_noalloc_scratch for the current device.  In host code
+// the symbol is only a host-side stand-in, so the address is looked up once
+// per device (first call on that device) and cached.
+bool noalloc_scratch(unsigned char** out) {
+  static std::mutex mu;
+  static unsigned char* addr[256] = {nullptr};
+  int dev = 0;
+  if (!VNEC_CUDA(cudaGetDevice(&dev))) return false;
+  if (dev < 0 || dev >= 256) {
+    set_error("SpB_mxv_csr_noalloc_ext: device ordinal out of range");
+    return false;
+  }
+  std::lock_guard<std::mutex> g(mu);
+  if (!addr[dev]) {
+    void* p = nullptr;
+    if (!VNEC_CUDA(cudaGetSymbolAddress(&p, g_noalloc_scratch))) return false;
+    addr[dev] = static_cast<unsigned char*>(p);
+  }
+  *out = addr[dev];
+  return true;
+}
+
+}  // namespace
+}  // namespace vnec
+
+extern "C" SpB_Info SpB_mxv_csr_noalloc_ext(int64_t n_rows, int64_t n_cols, int64_t nnz, const int32_t* d_row_ptr,
+                                            const int32_t* d_col, const double* d_val, const double* d_x,
+                                            double* d_y, void* stream) {
+  using namespace vnec;
+  clear_error();
+  if (n_rows < 0 || n_cols < 0 || nnz < 0) {
+    set_error("SpB_mxv_csr_noalloc_ext: negative size");
+    return SpB_FAILURE;
+  }
+  const long long ipc = (long long)kNaTpb * kNaIpt;
+  const long long tiles = (n_rows + nnz + ipc - 1) / ipc;
+  if (tiles > kNaMaxTiles) {
+    set_error("SpB_mxv_csr_noalloc_ext: n_rows + nnz exceeds the allocation-free limit of 469,762,048 "
+              "(its fixed scratch holds 262,144 tiles); use a plan (SpB_VNEC_plan_ext) instead");
+    return SpB_FAILURE;
+  }
+  if (n_rows == 0) return SpB_SUCCESS;
+  if (!d_row_ptr || !d_y || (nnz > 0 && (!d_col || !d_val || !d_x))) {
+    set_error("SpB_mxv_csr_noalloc_ext: NULL device array");
+    return SpB_FAILURE;
+  }
+  unsigned char* scratch = nullptr;
+  if (!noalloc_scratch(&scratch)) return SpB_FAILURE;
+  MpMatrix m;
+  m.n_rows = n_rows;
+  m.n_cols = n_cols;
+  m.nnz = nnz;
+  m.wide = false;
+  m.row_end = d_row_ptr + 1;
+  m.col = d_col;
+  m.val = d_val;
+  m.tile_row = scratch + kNaTileRowOff;
+  m.tile_nz = scratch + kNaTileNzOff;
+  m.carry_row = scratch + kNaCarryRowOff;
+  m.carry_val = scratch + kNaCarryValOff;
+  m.num_tiles = tiles;
+  m.shape.tpb = kNaTpb;
+  m.shape.ipt = kNaIpt;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  // Every scratch word a launch reads is written earlier in the same call
+  // (coordinates by the partition kernel, carries by the tile kernel), so
+  // nothing needs clearing between calls.
+  if (!mp_partition(m, s)) return SpB_FAILURE;
+  return mp_spmv(m, MpForm::kF64, d_x, d_y, s) ? SpB_SUCCESS : SpB_FAILURE;
+}
