@@ -70,6 +70,18 @@ struct VNEC_S_FP32 *Build_VNEC_S_FP32(const SpB_Matrix A);
 void SpMV_VNEC_S_FP64(SpB_Vector y, const SpB_Matrix A, const SpB_Vector x, VNEC_S_FP64 *mat_thd);
 void SpMV_VNEC_S_FP32(SpB_Vector y, const SpB_Matrix A, const SpB_Vector x, VNEC_S_FP32 *mat_thd);
 
+/* include/OpenSparseBLAS.h:2043 and :1982 (spmv_vnec_D_for_mxv.c:242-398,
+ * :2-241).  Dense-block plan: each row cut into zero-padded blocks of 4
+ * consecutive columns by the reference's grouping rule (applied to global
+ * columns), laid out as warp tasks like the sliced format.  Rows must have
+ * strictly increasing columns.  Release with VNEC_D_free_fp64 / _fp32. */
+struct VNEC_D_FP64 *Build_VNEC_D_FP64(const SpB_Matrix A);
+struct VNEC_D_FP32 *Build_VNEC_D_FP32(const SpB_Matrix A);
+
+/* include/OpenSparseBLAS.h:2038 and :1977 (spmv_vnec_D_for_mxv.c:400-485, :185-241). */
+void SpMV_VNEC_D_FP64(SpB_Vector y, const SpB_Matrix A, const SpB_Vector x, VNEC_D_FP64 *mat_thd);
+void SpMV_VNEC_D_FP32(SpB_Vector y, const SpB_Matrix A, const SpB_Vector x, VNEC_D_FP32 *mat_thd);
+
 /* ------------------------------------------------------------------------ */
 /* Handle release (the reference frees handles field by field in its test    */
 /* code, src/operation/test/test_spmv_vnec.hpp:81-176 and                     */
@@ -78,6 +90,8 @@ void SpMV_VNEC_S_FP32(SpB_Vector y, const SpB_Matrix A, const SpB_Vector x, VNEC
 void VNEC_L_free_ext(VNEC_L *mat_thd);
 void VNEC_S_free_fp64(VNEC_S_FP64 *mat_thd);
 void VNEC_S_free_fp32(VNEC_S_FP32 *mat_thd);
+void VNEC_D_free_fp64(VNEC_D_FP64 *mat_thd);
+void VNEC_D_free_fp32(VNEC_D_FP32 *mat_thd);
 
 /* ------------------------------------------------------------------------ */
 /* Extensions                                                                */
@@ -152,7 +166,8 @@ typedef struct {
   int64_t num_tiles;
   int pipeline_stages;     /* 0 for the unpipelined kernel */
   int arithmetic;          /* SpB_VNEC_arith_ext in use */
-  int reserved[6];
+  int64_t blocks;          /* dense-block plans: blocks of 4 columns (fill = nnz / (4 * blocks)) */
+  int reserved[4];
 } SpB_VNEC_info_ext;
 
 /* Device-side error status of the plan's last calls: waits for the plan's

@@ -345,3 +345,82 @@ def test_sliced_full_size_rmat_scale24(built):
     check_f64(y, m, xv)
     assert p.mxv_host(xv).tobytes() == y.tobytes()
     p.free()
+
+
+# ---------------------------------------------------------------------------
+# Dense-block kernel (VNEC-D counterpart)
+# ---------------------------------------------------------------------------
+
+@pytest.mark.parametrize("case", golden_cases())
+@pytest.mark.parametrize("fp64", [True, False])
+def test_golden_dense_dropin(built, case, fp64):
+    from vnec_gb300 import api
+
+    g = load_golden(case)
+    m = golden_csr(g)
+    dt = np.float64 if fp64 else np.float32
+    A = api.Matrix.from_csr(m, dtype=dt)
+    x = api.Vector(g["x"], dtype=dt)
+    y = api.Vector(np.full(m.n_rows, np.nan), dtype=dt)
+    if fp64:
+        h = api.Build_VNEC_D_FP64(A)
+        api.SpMV_VNEC_D_FP64(y, A, x, h)
+        api.VNEC_D_free_fp64(h)
+        if case.startswith("kat_"):
+            assert y.values.tobytes() == g["y_serial_f64"].tobytes()
+        else:
+            check_f64(y.values, m, g["x"])
+    else:
+        h = api.Build_VNEC_D_FP32(A)
+        api.SpMV_VNEC_D_FP32(y, A, x, h)
+        api.VNEC_D_free_fp32(h)
+        check_f32(y.values, m, g["x"])
+
+
+@pytest.mark.parametrize("kw", SLICED_PARAMS, ids=[str(k) for k in SLICED_PARAMS])
+def test_dense_params(built, kw):
+    from vnec_gb300 import api
+    from vnec_gb300 import generators as G
+
+    for m in (G.rmat(16, 16 << 16, seed=7), G.stencil27(20, seed=9), G.banded(5000, 65, seed=3),
+              G.blockdiag(4000, 24, seed=4)):
+        xv = G.vector(m.n_cols, seed=9)
+        p = api.Plan(m, kernel=api.KERNEL_D, **kw)
+        inf = p.info()
+        assert m.nnz <= 4 * inf.blocks
+        y = p.mxv_host(xv)
+        check_f64(y, m, xv)
+        assert p.mxv_host(xv).tobytes() == y.tobytes()
+        p.free()
+
+
+@pytest.mark.parametrize("name", ["empty_matrix", "single_row_spanning_tiles", "all_rows_empty",
+                                  "single_entry", "rectangular_wide", "rectangular_tall", "tile_boundary",
+                                  "hub_rows_and_empties"])
+def test_dense_edge_cases(built, name):
+    from vnec_gb300 import api
+
+    m = _edge_matrix(name)
+    xv = np.random.default_rng(2).uniform(-1, 1, size=m.n_cols)
+    for kw in (dict(), dict(long_row_len=40, window_rows=100)):
+        p = api.Plan(m, kernel=api.KERNEL_D, **kw)
+        check_f64(p.mxv_host(xv), m, xv)
+        p.free()
+
+
+def test_dense_blocks_reach_the_last_columns(built):
+    """Blocks starting in the last 3 columns read x only inside the matrix."""
+    from vnec_gb300 import api
+
+    n = 10
+    rows = [[7, 8, 9], [9], [0, 3, 6, 9], [8, 9], [5, 9]]
+    row_ptr = np.cumsum([0] + [len(r) for r in rows]).astype(np.int64)
+    col = np.concatenate(rows).astype(np.int32)
+    val = np.arange(1, len(col) + 1, dtype=np.float64)
+    from vnec_gb300 import generators as G
+
+    m = G.from_arrays(len(rows), n, row_ptr, col, val)
+    xv = np.arange(1, n + 1, dtype=np.float64)
+    p = api.Plan(m, kernel=api.KERNEL_D)
+    assert np.array_equal(p.mxv_host(xv), m.to_dense() @ xv)
+    p.free()

@@ -71,7 +71,7 @@ class Info(C.Structure):
                 ("nnz", C.c_int64), ("device_bytes", C.c_int64), ("algorithmic_bytes", C.c_int64),
                 ("launches_per_call", C.c_int), ("threads_per_block", C.c_int), ("items_per_thread", C.c_int),
                 ("num_tiles", C.c_int64), ("pipeline_stages", C.c_int), ("arithmetic", C.c_int),
-                ("reserved", C.c_int * 6)]
+                ("blocks", C.c_int64), ("reserved", C.c_int * 4)]
 
 
 _vp = C.c_void_p
@@ -88,13 +88,14 @@ def lib() -> C.CDLL:
     L.IRD_VNEC.restype = C.c_int
     L.Build_VNEC_L.argtypes = [_vp]
     L.Build_VNEC_L.restype = _vp
-    for f in ("SpMV_VNEC_L_FP64", "SpMV_VNEC_L_FP32", "SpMV_VNEC_S_FP64", "SpMV_VNEC_S_FP32"):
+    for f in ("SpMV_VNEC_L_FP64", "SpMV_VNEC_L_FP32", "SpMV_VNEC_S_FP64", "SpMV_VNEC_S_FP32",
+              "SpMV_VNEC_D_FP64", "SpMV_VNEC_D_FP32"):
         getattr(L, f).argtypes = [_vp, _vp, _vp, _vp]
         getattr(L, f).restype = None
-    for f in ("Build_VNEC_S_FP64", "Build_VNEC_S_FP32"):
+    for f in ("Build_VNEC_S_FP64", "Build_VNEC_S_FP32", "Build_VNEC_D_FP64", "Build_VNEC_D_FP32"):
         getattr(L, f).argtypes = [_vp]
         getattr(L, f).restype = _vp
-    for f in ("VNEC_L_free_ext", "VNEC_S_free_fp64", "VNEC_S_free_fp32"):
+    for f in ("VNEC_L_free_ext", "VNEC_S_free_fp64", "VNEC_S_free_fp32", "VNEC_D_free_fp64", "VNEC_D_free_fp32"):
         getattr(L, f).argtypes = [_vp]
         getattr(L, f).restype = None
     L.SpB_VNEC_last_error_ext.argtypes = []
@@ -240,6 +241,36 @@ def SpMV_VNEC_S_FP64(y: Vector, A: Matrix, x: Vector, h: int) -> None:
 def SpMV_VNEC_S_FP32(y: Vector, A: Matrix, x: Vector, h: int) -> None:
     lib().SpMV_VNEC_S_FP32(y.handle, A.handle, x.handle, h)
     _check(last_error() == "", "SpMV_VNEC_S_FP32")
+
+
+def Build_VNEC_D_FP64(A: Matrix) -> int:
+    h = lib().Build_VNEC_D_FP64(A.handle)
+    _check(bool(h), "Build_VNEC_D_FP64")
+    return h
+
+
+def Build_VNEC_D_FP32(A: Matrix) -> int:
+    h = lib().Build_VNEC_D_FP32(A.handle)
+    _check(bool(h), "Build_VNEC_D_FP32")
+    return h
+
+
+def SpMV_VNEC_D_FP64(y: Vector, A: Matrix, x: Vector, h: int) -> None:
+    lib().SpMV_VNEC_D_FP64(y.handle, A.handle, x.handle, h)
+    _check(last_error() == "", "SpMV_VNEC_D_FP64")
+
+
+def SpMV_VNEC_D_FP32(y: Vector, A: Matrix, x: Vector, h: int) -> None:
+    lib().SpMV_VNEC_D_FP32(y.handle, A.handle, x.handle, h)
+    _check(last_error() == "", "SpMV_VNEC_D_FP32")
+
+
+def VNEC_D_free_fp64(h: int) -> None:
+    lib().VNEC_D_free_fp64(h)
+
+
+def VNEC_D_free_fp32(h: int) -> None:
+    lib().VNEC_D_free_fp32(h)
 
 
 def VNEC_S_free_fp64(h: int) -> None:

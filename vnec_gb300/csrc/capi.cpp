@@ -60,6 +60,23 @@ Pub* publish_s(std::unique_ptr<Plan> plan) {
 }
 
 template <typename Pub>
+Pub* publish_d(std::unique_ptr<Plan> plan) {
+  if (plan) plan->pub_part_arrays = true;
+  Pub* pub = publish<Pub>(std::move(plan));
+  if (pub) fill_part_arrays(pub);
+  return pub;
+}
+
+template <typename Pub>
+void free_d(Pub* pub) {
+  if (!pub) return;
+  std::unique_ptr<Plan> p = take_plan(pub);
+  if (!p) return;
+  free_part_arrays(pub);
+  std::free(pub);
+}
+
+template <typename Pub>
 void free_s(Pub* pub) {
   if (!pub) return;
   std::unique_ptr<Plan> p = take_plan(pub);
@@ -125,6 +142,8 @@ std::unique_ptr<Plan> build_from_view(const CsrView& v, const SpB_VNEC_options_e
       return build_merge_path(v, opts);
     case SpB_VNEC_KERNEL_S:
       return build_sliced(v, opts);
+    case SpB_VNEC_KERNEL_D:
+      return build_dense(v, opts);
     default:
       set_error("requested kernel is not available");
       return nullptr;
@@ -286,6 +305,43 @@ void SpMV_VNEC_S_FP32(SpB_Vector y, const SpB_Matrix A, const SpB_Vector x, VNEC
 void VNEC_S_free_fp64(VNEC_S_FP64* mat_thd) { free_s(mat_thd); }
 void VNEC_S_free_fp32(VNEC_S_FP32* mat_thd) { free_s(mat_thd); }
 
+struct VNEC_D_FP64* Build_VNEC_D_FP64(const SpB_Matrix A) {
+  clear_error();
+  CsrView v;
+  if (!view_from_matrix(A, &v)) return nullptr;
+  if (v.type != SpB_FP64) {
+    set_error("Build_VNEC_D_FP64: matrix is not FP64");
+    return nullptr;
+  }
+  return publish_d<VNEC_D_FP64>(build_dense(v, nullptr));
+}
+
+struct VNEC_D_FP32* Build_VNEC_D_FP32(const SpB_Matrix A) {
+  clear_error();
+  CsrView v;
+  if (!view_from_matrix(A, &v)) return nullptr;
+  if (v.type != SpB_FP32) {
+    set_error("Build_VNEC_D_FP32: matrix is not FP32");
+    return nullptr;
+  }
+  return publish_d<VNEC_D_FP32>(build_dense(v, nullptr));
+}
+
+void SpMV_VNEC_D_FP64(SpB_Vector y, const SpB_Matrix A, const SpB_Vector x, VNEC_D_FP64* mat_thd) {
+  clear_error();
+  Plan* p = typed_plan(mat_thd, SpB_FP64, PlanKind::kWindowDense, "SpMV_VNEC_D_FP64");
+  if (p) run_mxv(y, A, x, p);
+}
+
+void SpMV_VNEC_D_FP32(SpB_Vector y, const SpB_Matrix A, const SpB_Vector x, VNEC_D_FP32* mat_thd) {
+  clear_error();
+  Plan* p = typed_plan(mat_thd, SpB_FP32, PlanKind::kWindowDense, "SpMV_VNEC_D_FP32");
+  if (p) run_mxv(y, A, x, p);
+}
+
+void VNEC_D_free_fp64(VNEC_D_FP64* mat_thd) { free_d(mat_thd); }
+void VNEC_D_free_fp32(VNEC_D_FP32* mat_thd) { free_d(mat_thd); }
+
 const char* SpB_VNEC_last_error_ext(void) { return last_error(); }
 
 void* SpB_VNEC_plan_ext(const SpB_VNEC_options_ext* opts, SpB_Type type, int64_t n_rows, int64_t n_cols,
@@ -316,6 +372,13 @@ void SpB_VNEC_plan_free_ext(void* plan) {
       free_s(static_cast<VNEC_S_FP64*>(plan));
     else
       free_s(static_cast<VNEC_S_FP32*>(plan));
+    return;
+  }
+  if (p->pub_part_arrays && p->kind == PlanKind::kWindowDense) {
+    if (p->type == SpB_FP64)
+      free_d(static_cast<VNEC_D_FP64*>(plan));
+    else
+      free_d(static_cast<VNEC_D_FP32*>(plan));
     return;
   }
   take_plan(plan);

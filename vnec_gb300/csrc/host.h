@@ -81,6 +81,7 @@ std::unique_ptr<Plan> take_plan(const void* handle);
 // Plan builders.
 std::unique_ptr<Plan> build_merge_path(const CsrView& v, const SpB_VNEC_options_ext* opts);
 std::unique_ptr<Plan> build_sliced(const CsrView& v, const SpB_VNEC_options_ext* opts);
+std::unique_ptr<Plan> build_dense(const CsrView& v, const SpB_VNEC_options_ext* opts);
 
 // Reference partition count and lane width constants used by IRD_VNEC.
 struct IrdParams {

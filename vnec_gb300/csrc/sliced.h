@@ -28,13 +28,14 @@ struct SlicedMatrix {
   int64_t n_rows = 0, n_cols = 0, nnz = 0, entries = 0;  // entries include padding
   int64_t num_tasks = 0, num_long = 0, num_chunks = 0;
   const SlicedTask* tasks = nullptr;
-  const void* val = nullptr;        // entries (double or float), padding = 0
+  const void* val = nullptr;        // entries x vpe values (double or float), padding = 0
   const int32_t* col = nullptr;     // entries, padding = a valid column
   const int32_t* rowid = nullptr;   // group row slots
   const int32_t* long_row = nullptr;    // num_long rows
   const int32_t* long_first = nullptr;  // num_long + 1 chunk offsets
   void* chunk_sum = nullptr;            // num_chunks scratch (value type)
   int cache_hints = 0;                  // 0: streaming/read-only defaults, 1: explicit L1/L2 policies
+  int vpe = 1;                          // values per entry: 1 (nonzeros) or 4 (dense blocks)
 };
 
 struct SlicedParams {
@@ -46,9 +47,13 @@ struct SlicedParams {
 
 // Host-side arrays of a built sliced matrix.
 struct SlicedHost;
+// `vpe` values per entry: 1 for the sliced format (one nonzero per entry),
+// the block width for the dense-block format (entry = block start column +
+// that many consecutive zero-padded values).
 SlicedHost* sliced_build(int64_t n_rows, int64_t n_cols, const int64_t* row_ptr_or_null,
                          const uint64_t* row_ptr64_or_null, const int32_t* col_or_null,
-                         const uint64_t* col64_or_null, const void* val, int value_bytes, const SlicedParams& prm);
+                         const uint64_t* col64_or_null, const void* val, int value_bytes, const SlicedParams& prm,
+                         int vpe = 1);
 void sliced_free(SlicedHost* h);
 // Uploads a built matrix; device buffers are owned by the caller-provided allocator.
 struct SlicedHostView {
@@ -59,6 +64,7 @@ struct SlicedHostView {
   const int32_t* rowid;
   const int32_t* long_row;
   const int32_t* long_first;
+  int vpe;
 };
 SlicedHostView sliced_view(const SlicedHost* h);
 

@@ -25,6 +25,7 @@ namespace vnec {
 
 struct SlicedHost {
   int64_t entries = 0, n_rowid = 0, num_long = 0, num_chunks = 0;
+  int vpe = 1;
   std::vector<SlicedTask> tasks;
   std::unique_ptr<unsigned char[]> val;
   std::unique_ptr<int32_t[]> col;
@@ -55,7 +56,10 @@ inline int meta(int kind, int vwl, int nrows) { return kind | (vwl << 4) | (nrow
 }  // namespace
 
 SlicedHost* sliced_build(int64_t n_rows, int64_t n_cols, const int64_t* rp, const uint64_t* rp64, const int32_t* ci,
-                         const uint64_t* ci64, const void* val, int vb, const SlicedParams& prm) {
+                         const uint64_t* ci64, const void* val, int vb, const SlicedParams& prm, int vpe) {
+  // Each entry carries `vpe` consecutive values (1 for single nonzeros, the
+  // block width for dense blocks); `vb` is the size of one value.
+  const int eb = vb * vpe;
   auto begin = [&](int64_t r) -> int64_t { return rp ? rp[r] : (int64_t)rp64[r]; };
   auto colat = [&](int64_t p) -> int32_t { return ci ? ci[p] : (int32_t)ci64[p]; };
   const int64_t W = prm.window_rows;
@@ -144,9 +148,10 @@ SlicedHost* sliced_build(int64_t n_rows, int64_t n_cols, const int64_t* rp, cons
   h->long_row.resize((size_t)off_l[nwin]);
   h->long_first.resize((size_t)off_l[nwin] + 1);
   const int64_t pad = 64;
-  h->val.reset(new unsigned char[(size_t)(h->entries + pad) * vb]);
+  h->val.reset(new unsigned char[(size_t)(h->entries + pad) * eb]);
   h->col.reset(new int32_t[(size_t)(h->entries + pad)]);
-  std::memset(h->val.get() + (size_t)h->entries * vb, 0, (size_t)pad * vb);
+  h->vpe = vpe;
+  std::memset(h->val.get() + (size_t)h->entries * eb, 0, (size_t)pad * eb);
   std::memset(h->col.get() + h->entries, 0, sizeof(int32_t) * pad);
 
   // Pass 2: global task list and the interleaved entries.
@@ -174,9 +179,9 @@ SlicedHost* sliced_build(int64_t n_rows, int64_t n_cols, const int64_t* rp, cons
       if (kind == kSlicedZero) continue;
       const int64_t vw = (int64_t)1 << vwl;
       const int64_t span = (int64_t)t.steps * 32;
-      unsigned char* vdst = h->val.get() + (size_t)t.base * vb;
+      unsigned char* vdst = h->val.get() + (size_t)t.base * eb;
       int32_t* cdst = h->col.get() + t.base;
-      std::memset(vdst, 0, (size_t)span * vb);
+      std::memset(vdst, 0, (size_t)span * eb);
       if (kind == kSlicedRows) {
         const int32_t pad_col = 0;
         for (int64_t e = 0; e < span; ++e) cdst[e] = pad_col;
@@ -186,7 +191,7 @@ SlicedHost* sliced_build(int64_t n_rows, int64_t n_cols, const int64_t* rp, cons
           for (int64_t j = 0; j < len; ++j) {
             const int64_t pos = (j >> vwl) * 32 + g * vw + (j & (vw - 1));
             cdst[pos] = colat(b + j);
-            std::memcpy(vdst + pos * vb, static_cast<const unsigned char*>(val) + (b + j) * vb, (size_t)vb);
+            std::memcpy(vdst + pos * eb, static_cast<const unsigned char*>(val) + (b + j) * eb, (size_t)eb);
           }
         }
       } else {  // chunk of a long row
@@ -196,7 +201,7 @@ SlicedHost* sliced_build(int64_t n_rows, int64_t n_cols, const int64_t* rp, cons
         for (int64_t e = 0; e < span; ++e) cdst[e] = colat(b + lo);
         for (int64_t j = lo; j < hi; ++j) {
           cdst[j - lo] = colat(b + j);
-          std::memcpy(vdst + (j - lo) * vb, static_cast<const unsigned char*>(val) + (b + j) * vb, (size_t)vb);
+          std::memcpy(vdst + (j - lo) * eb, static_cast<const unsigned char*>(val) + (b + j) * eb, (size_t)eb);
         }
         if (++chunk_in_row == wd.long_nchunks[li]) {
           chunk_in_row = 0;
@@ -224,6 +229,7 @@ SlicedHostView sliced_view(const SlicedHost* h) {
   v.rowid = h->rowid.data();
   v.long_row = h->long_row.data();
   v.long_first = h->long_first.data();
+  v.vpe = h->vpe;
   return v;
 }
 

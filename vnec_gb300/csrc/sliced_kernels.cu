@@ -69,9 +69,75 @@ template <int H, typename T> __device__ __forceinline__ T ld_x_h(const T* p, con
   if constexpr (H == 0) return __ldg(p); else return ld_keep(p, pol.keep);
 }
 
+
 template <typename V> __device__ __forceinline__ V fmav(V a, V b, V c);
 template <> __device__ __forceinline__ double fmav<double>(double a, double b, double c) { return fma(a, b, c); }
 template <> __device__ __forceinline__ float fmav<float>(float a, float b, float c) { return fmaf(a, b, c); }
+
+// Dense-block entries (VNEC-D counterpart): 4 consecutive values starting at
+// column c; x is read at c..c+3 (guarded by n_cols).
+template <typename V> struct Quad;
+template <> struct Quad<double> {
+  __device__ static void load(const double* p, double (&v)[4]) {
+    const double2 a = __ldcs(reinterpret_cast<const double2*>(p));
+    const double2 b = __ldcs(reinterpret_cast<const double2*>(p) + 1);
+    v[0] = a.x; v[1] = a.y; v[2] = b.x; v[3] = b.y;
+  }
+};
+template <> struct Quad<float> {
+  __device__ static void load(const float* p, float (&v)[4]) {
+    const float4 a = __ldcs(reinterpret_cast<const float4*>(p));
+    v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
+  }
+};
+
+template <typename V>
+__device__ __forceinline__ V block_dot(const V* vp, int c, const V* __restrict__ x, int n_cols, V acc) {
+  V v[4];
+  Quad<V>::load(vp, v);
+#pragma unroll
+  for (int l = 0; l < 4; ++l) {
+    const V xv = (c + l < n_cols) ? __ldg(x + c + l) : V(0);
+    acc = fmav<V>(v[l], xv, acc);
+  }
+  return acc;
+}
+
+template <typename V>
+__global__ void __launch_bounds__(kWarpsPerBlock * 32)
+dense_block_kernel(const SlicedTask* __restrict__ tasks, long long num_tasks, const V* __restrict__ val,
+                   const int32_t* __restrict__ col, const int32_t* __restrict__ rowid, const V* __restrict__ x,
+                   int n_cols, V* __restrict__ y, V* __restrict__ chunk_sum) {
+  const long long w = ((long long)blockIdx.x * kWarpsPerBlock) + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  if (w >= num_tasks) return;
+  const int4 raw = __ldg(reinterpret_cast<const int4*>(tasks) + w);
+  const int base = raw.x, row_base = raw.y, steps = raw.z, meta = raw.w;
+  const int kind = meta & 15, vwl = (meta >> 4) & 15, nrows = meta >> 8;
+  if (kind == kSlicedZero) {
+    if (lane < nrows) y[rowid[row_base + lane]] = V(0);
+    return;
+  }
+  const V* vp = val + (size_t)(base + lane) * 4;
+  const int32_t* cp = col + base + lane;
+  V acc = V(0);
+  int k = 0;
+  for (; k + 4 <= steps; k += 4) {
+    int c[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) c[u] = __ldcs(cp + (k + u) * 32);
+#pragma unroll
+    for (int u = 0; u < 4; ++u) acc = block_dot<V>(vp + (size_t)(k + u) * 128, c[u], x, n_cols, acc);
+  }
+  for (; k < steps; ++k) acc = block_dot<V>(vp + (size_t)k * 128, __ldcs(cp + k * 32), x, n_cols, acc);
+  for (int off = (1 << vwl) >> 1; off > 0; off >>= 1) acc += __shfl_xor_sync(kFull, acc, off);
+  if (kind == kSlicedChunk) {
+    if (lane == 0) chunk_sum[row_base] = acc;
+  } else {
+    const int g = lane >> vwl;
+    if ((lane & ((1 << vwl) - 1)) == 0 && g < nrows) y[rowid[row_base + g]] = acc;
+  }
+}
 
 template <typename V, int U, int H>
 __global__ void __launch_bounds__(kWarpsPerBlock * 32)
@@ -127,6 +193,19 @@ __global__ void sliced_long_fixup(const int32_t* __restrict__ long_row, const in
   y[long_row[i]] = s;
 }
 
+template <typename V>
+bool launch_dense(const SlicedMatrix& m, const void* x, void* y, cudaStream_t s) {
+  const long long grid = (m.num_tasks + kWarpsPerBlock - 1) / kWarpsPerBlock;
+  if (grid > 0x7fffffffLL) {
+    set_error("dense blocks: too many tasks for one launch");
+    return false;
+  }
+  dense_block_kernel<V><<<(unsigned)grid, kWarpsPerBlock * 32, 0, s>>>(
+      m.tasks, m.num_tasks, static_cast<const V*>(m.val), m.col, m.rowid, static_cast<const V*>(x), (int)m.n_cols,
+      static_cast<V*>(y), static_cast<V*>(m.chunk_sum));
+  return VNEC_CUDA(cudaGetLastError());
+}
+
 template <typename V, int H>
 bool launch_main(const SlicedMatrix& m, const void* x, void* y, cudaStream_t s) {
   auto kern = sliced_kernel<V, 8, H>;
@@ -151,7 +230,9 @@ template <typename V>
 bool launch(const SlicedMatrix& m, const void* x, void* y, cudaStream_t s, cudaEvent_t* ev) {
   if (ev && !VNEC_CUDA(cudaEventRecord(ev[0], s))) return false;
   if (m.num_tasks > 0) {
-    const bool ok = m.cache_hints ? launch_main<V, 1>(m, x, y, s) : launch_main<V, 0>(m, x, y, s);
+    const bool ok = m.vpe == 4       ? launch_dense<V>(m, x, y, s)
+                    : m.cache_hints ? launch_main<V, 1>(m, x, y, s)
+                                    : launch_main<V, 0>(m, x, y, s);
     if (!ok) return false;
   }
   if (ev && !VNEC_CUDA(cudaEventRecord(ev[1], s))) return false;
