@@ -127,8 +127,20 @@ typedef struct {
   int long_row_len;      /* sliced: rows longer than this are chunked (0: 1024) */
   int max_steps;         /* sliced: max 32-wide loads per lane for a row group (0: 32) */
   int cache_hints;       /* sliced: 0 default (streaming loads), 2 explicit L1/L2 evict policies */
-  int reserved[7];
+  int precision;         /* sliced, FP64 matrices: SpB_VNEC_precision_ext */
+  int reserved[6];
 } SpB_VNEC_options_ext;
+
+/* Precision forms of the sliced kernel for an FP64 matrix (x and y stay
+ * FP64).  Products are accumulated in FP32 per lane; row reductions, the
+ * BF16 row scale and the long-row fix-up are FP64. */
+typedef enum {
+  SpB_VNEC_PREC_FP64 = 0, /* plain: FP64 values, FP64 FMA */
+  SpB_VNEC_PREC_FP32 = 1, /* FP32 values (4 B), x rounded to FP32 per call */
+  SpB_VNEC_PREC_BF16 = 2, /* BF16 values (2 B) scaled per row by a power of two */
+  SpB_VNEC_PREC_DF32 = 3  /* FP32 hi+lo split of FP64 values and x, double-float
+                             sums: FP64-level error on the FP32 pipe */
+} SpB_VNEC_precision_ext;
 
 /* Plan from raw host CSR arrays: int64 row offsets (n_rows + 1), int32
  * columns and FP64/FP32 values (nnz = row_ptr[n_rows]).  The arrays are
@@ -167,13 +179,18 @@ typedef struct {
   int pipeline_stages;     /* 0 for the unpipelined kernel */
   int arithmetic;          /* SpB_VNEC_arith_ext in use */
   int64_t blocks;          /* dense-block plans: blocks of 4 columns (fill = nnz / (4 * blocks)) */
-  int reserved[4];
+  int precision;           /* SpB_VNEC_precision_ext of a sliced plan */
+  int reserved[3];
 } SpB_VNEC_info_ext;
 
 /* Device-side error status of the plan's last calls: waits for the plan's
  * work on `stream`, returns SpB_FAILURE (with a message) if a bounded
  * pipeline wait timed out, and clears the status. */
 SpB_Info SpB_VNEC_device_status_ext(void *plan, void *stream);
+
+/* Rounds n FP64 values to FP32 (round to nearest even) on `stream`; used for
+ * the FP32/BF16 precision forms, exposed for callers keeping x in FP32. */
+SpB_Info SpB_VNEC_f64_to_f32_ext(const double *d_in, float *d_out, int64_t n, void *stream);
 
 /* Allocation-free y := A x (no counterpart in the reference).
  *

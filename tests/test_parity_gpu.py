@@ -424,3 +424,88 @@ def test_dense_blocks_reach_the_last_columns(built):
     p = api.Plan(m, kernel=api.KERNEL_D)
     assert np.array_equal(p.mxv_host(xv), m.to_dense() @ xv)
     p.free()
+
+
+# ---------------------------------------------------------------------------
+# Precision forms of the sliced kernel (values FP32 / BF16 + row scale /
+# FP32 hi+lo double-float), FP64 x and y
+# ---------------------------------------------------------------------------
+
+# Row-wise bounds |y - yhat| <= tol * sum|a x| against the FP64 oracle, from
+# the stored value precision: FP32 2^-24 (plus FP32 x and sums), BF16 2^-9,
+# double-float ~2^-46.
+PREC_TOL = {1: 1e-6, 2: 1e-2, 3: 1e-12}
+
+
+@pytest.mark.parametrize("prec", [1, 2, 3], ids=["fp32", "bf16_rowscale", "df32_hilo"])
+def test_precision_forms_error_bounds(built, prec):
+    from vnec_gb300 import api
+    from vnec_gb300 import generators as G
+
+    for m in (G.rmat(16, 16 << 16, seed=7), G.lognormal(20000, sigma=2.5, cap=4096, seed=8),
+              G.stencil27(20, seed=9)):
+        xv = G.vector(m.n_cols, seed=9)
+        p = api.Plan(m, kernel=api.KERNEL_S, precision=prec)
+        assert p.info().precision == prec
+        y = p.mxv_host(xv)
+        check_f64(y, m, xv, tol=PREC_TOL[prec])
+        assert p.mxv_host(xv).tobytes() == y.tobytes()
+        p.free()
+
+
+def test_bf16_row_scale_handles_wide_row_magnitudes(built):
+    """Rows of very different magnitude: the power-of-two row scale keeps each
+    row's relative error at BF16 precision."""
+    from vnec_gb300 import api
+    from vnec_gb300 import generators as G
+
+    m = G.uniform_k(3000, 12, seed=3).copy()
+    rows = np.repeat(np.arange(m.n_rows), np.diff(m.row_ptr))
+    m.val[:] = m.val * np.exp2((rows % 60) - 30.0)
+    xv = G.vector(m.n_cols, seed=4)
+    p = api.Plan(m, kernel=api.KERNEL_S, precision=api.PREC_BF16)
+    check_f64(p.mxv_host(xv), m, xv, tol=PREC_TOL[2])
+    p.free()
+
+
+def test_df32_form_guard_for_out_of_range_x(built):
+    from vnec_gb300 import api
+    from vnec_gb300 import generators as G
+
+    m = G.rmat(15, 16 << 15, seed=3)
+    p = api.Plan(m, kernel=api.KERNEL_S, precision=api.PREC_DF32)
+    for bad in (1e30, 3e-20, 5e-324):
+        xv = G.vector(m.n_cols, seed=4)
+        xv[::97] = bad
+        check_f64(p.mxv_host(xv), m, xv)
+        xg = G.vector(m.n_cols, seed=5)
+        check_f64(p.mxv_host(xg), m, xg)
+    p.free()
+
+
+def test_f64_to_f32_rounding_matches_hardware(built):
+    """The integer round-to-nearest-even conversion against CUDA's own
+    conversion (torch's .float() on the device) on random and special values."""
+    import torch
+
+    from vnec_gb300 import api
+
+    rng = np.random.default_rng(11)
+    bits = rng.integers(0, 2 ** 63, size=1 << 20, dtype=np.uint64) | (rng.integers(0, 2, size=1 << 20,
+                                                                                  dtype=np.uint64) << 63)
+    vals = bits.view(np.float64)
+    specials = np.array([0.0, -0.0, np.inf, -np.inf, np.nan, 1.0, -1.0, 3.4028234663852886e38,
+                         3.4028235677973366e38, 1.401298464324817e-45, 7.006492321624085e-46,
+                         1.1754942106924411e-38, 1.1754943508222875e-38, 2.0 ** -149, 2.0 ** -150,
+                         1.0 + 2.0 ** -24, 1.0 + 3 * 2.0 ** -24, 5e-324, -1e-310])
+    near = (np.float32(rng.uniform(-1e3, 1e3, 4096)).astype(np.float64) *
+            (1 + rng.choice([2.0 ** -24, -2.0 ** -24, 2.0 ** -25], 4096)))
+    allv = np.concatenate([vals, specials, near])
+    d = torch.from_numpy(allv).cuda()
+    out = torch.empty(allv.size, dtype=torch.float32, device="cuda")
+    assert api.lib().SpB_VNEC_f64_to_f32_ext(d.data_ptr(), out.data_ptr(), allv.size, None) == api.SpB_SUCCESS
+    ref = d.float().cpu().numpy()
+    got = out.cpu().numpy()
+    nan = np.isnan(ref)
+    assert np.array_equal(np.isnan(got), nan)
+    assert np.array_equal(got[~nan].view(np.uint32), ref[~nan].view(np.uint32))

@@ -27,6 +27,7 @@ SpB_CSC, SpB_CSR = 0, 1
 SpB_VNEC_D, SpB_VNEC_S = 0, 1
 KERNEL_AUTO, KERNEL_L, KERNEL_D, KERNEL_S = 0, 1, 2, 3
 ARITH_AUTO, ARITH_FP64, ARITH_DF32 = 0, 1, 2
+PREC_FP64, PREC_FP32, PREC_BF16, PREC_DF32 = 0, 1, 2, 3
 
 _DTYPE = {SpB_FP32: np.float32, SpB_FP64: np.float64}
 
@@ -61,7 +62,7 @@ class Options(C.Structure):
     _fields_ = [("kernel", C.c_int), ("threads_per_block", C.c_int), ("items_per_thread", C.c_int),
                 ("pipeline_stages", C.c_int), ("arithmetic", C.c_int), ("window_rows", C.c_int),
                 ("long_row_len", C.c_int), ("max_steps", C.c_int), ("cache_hints", C.c_int),
-                ("reserved", C.c_int * 7)]
+                ("precision", C.c_int), ("reserved", C.c_int * 6)]
 
 
 class Info(C.Structure):
@@ -71,7 +72,7 @@ class Info(C.Structure):
                 ("nnz", C.c_int64), ("device_bytes", C.c_int64), ("algorithmic_bytes", C.c_int64),
                 ("launches_per_call", C.c_int), ("threads_per_block", C.c_int), ("items_per_thread", C.c_int),
                 ("num_tiles", C.c_int64), ("pipeline_stages", C.c_int), ("arithmetic", C.c_int),
-                ("blocks", C.c_int64), ("reserved", C.c_int * 4)]
+                ("blocks", C.c_int64), ("precision", C.c_int), ("reserved", C.c_int * 3)]
 
 
 _vp = C.c_void_p
@@ -120,6 +121,8 @@ def lib() -> C.CDLL:
     L.SpB_VNEC_kernel_ms_ext.restype = C.c_int
     L.SpB_VNEC_device_status_ext.argtypes = [_vp, _vp]
     L.SpB_VNEC_device_status_ext.restype = C.c_int
+    L.SpB_VNEC_f64_to_f32_ext.argtypes = [_vp, _vp, C.c_int64, _vp]
+    L.SpB_VNEC_f64_to_f32_ext.restype = C.c_int
     L._vnec_typed = True
     return L
 
@@ -289,12 +292,12 @@ def SpB_mxv(y: Vector, A: Matrix, x: Vector, vnec: int | None = None) -> None:
 
 def options(kernel: int = KERNEL_AUTO, threads_per_block: int = 0, items_per_thread: int = 0,
             pipeline_stages: int = 0, arithmetic: int = ARITH_AUTO, window_rows: int = 0, long_row_len: int = 0,
-            max_steps: int = 0, cache_hints: int = 0) -> Options:
+            max_steps: int = 0, cache_hints: int = 0, precision: int = PREC_FP64) -> Options:
     o = Options()
     o.kernel, o.threads_per_block, o.items_per_thread = kernel, threads_per_block, items_per_thread
     o.pipeline_stages, o.arithmetic = pipeline_stages, arithmetic
     o.window_rows, o.long_row_len, o.max_steps = window_rows, long_row_len, max_steps
-    o.cache_hints = cache_hints
+    o.cache_hints, o.precision = cache_hints, precision
     return o
 
 

@@ -70,6 +70,23 @@ SlicedHostView sliced_view(const SlicedHost* h);
 
 bool sliced_spmv(const SlicedMatrix& m, bool fp64, const void* x, void* y, cudaStream_t s,
                  cudaEvent_t* events = nullptr);
+
+// Precision forms of the sliced format (sliced_mixed.cu).
+enum SlicedPrecision : int { kPrecFP64 = 0, kPrecFP32 = 1, kPrecBF16 = 2, kPrecDF32 = 3 };
+struct SlicedMixed {
+  int precision = kPrecFP64;
+  void* xbuf = nullptr;                    // n_cols converted x: float (FP32/BF16) or float2 (DF32)
+  int* flag = nullptr;                     // DF32: x outside the split range this call
+  const signed char* row_scale = nullptr;  // BF16: power-of-two exponent per row slot
+  const signed char* chunk_scale = nullptr;  // BF16: exponent per chunk
+};
+bool sliced_mixed_spmv(const SlicedMatrix& m, const SlicedMixed& mx, const double* x, double* y, cudaStream_t s,
+                       cudaEvent_t* events = nullptr);
+// FP64 sliced kernel that only runs when *flag != 0 (DF32 fallback).
+bool sliced_guard_f64(const SlicedMatrix& m, const double* x, double* y, const int* flag, cudaStream_t s);
+inline int sliced_mixed_launches(const SlicedMatrix& m, int precision) {
+  return 2 + (precision == kPrecDF32 ? 1 : 0) + (m.num_long > 0 || precision == kPrecDF32 ? 1 : 0);
+}
 inline int sliced_launches(const SlicedMatrix& m) { return m.num_long > 0 ? 2 : 1; }
 
 }  // namespace vnec

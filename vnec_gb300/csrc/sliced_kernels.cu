@@ -143,7 +143,8 @@ template <typename V, int U, int H>
 __global__ void __launch_bounds__(kWarpsPerBlock * 32)
 sliced_kernel(const SlicedTask* __restrict__ tasks, long long num_tasks, const V* __restrict__ val,
               const int32_t* __restrict__ col, const int32_t* __restrict__ rowid, const V* __restrict__ x,
-              V* __restrict__ y, V* __restrict__ chunk_sum) {
+              V* __restrict__ y, V* __restrict__ chunk_sum, const int* __restrict__ guard = nullptr) {
+  if (guard && *reinterpret_cast<const volatile int*>(guard) == 0) return;
   const long long w = ((long long)blockIdx.x * kWarpsPerBlock) + (threadIdx.x >> 5);
   const int lane = threadIdx.x & 31;
   if (w >= num_tasks) return;
@@ -222,7 +223,7 @@ bool launch_main(const SlicedMatrix& m, const void* x, void* y, cudaStream_t s) 
   }
   kern<<<(unsigned)grid, kWarpsPerBlock * 32, 0, s>>>(m.tasks, m.num_tasks, static_cast<const V*>(m.val), m.col,
                                                       m.rowid, static_cast<const V*>(x), static_cast<V*>(y),
-                                                      static_cast<V*>(m.chunk_sum));
+                                                      static_cast<V*>(m.chunk_sum), nullptr);
   return VNEC_CUDA(cudaGetLastError());
 }
 
@@ -247,6 +248,14 @@ bool launch(const SlicedMatrix& m, const void* x, void* y, cudaStream_t s, cudaE
 }
 
 }  // namespace
+
+bool sliced_guard_f64(const SlicedMatrix& m, const double* x, double* y, const int* flag, cudaStream_t s) {
+  const long long grid = (m.num_tasks + kWarpsPerBlock - 1) / kWarpsPerBlock;
+  sliced_kernel<double, 8, 0><<<(unsigned)grid, kWarpsPerBlock * 32, 0, s>>>(
+      m.tasks, m.num_tasks, static_cast<const double*>(m.val), m.col, m.rowid, x, y,
+      static_cast<double*>(m.chunk_sum), flag);
+  return VNEC_CUDA(cudaGetLastError());
+}
 
 bool sliced_spmv(const SlicedMatrix& m, bool fp64, const void* x, void* y, cudaStream_t s, cudaEvent_t* ev) {
   return fp64 ? launch<double>(m, x, y, s, ev) : launch<float>(m, x, y, s, ev);

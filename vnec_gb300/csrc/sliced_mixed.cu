@@ -1,0 +1,304 @@
+// Precision forms of the sliced row-group SpMV (same warp-task layout as
+// sliced_kernels.cu), all producing FP64 y from FP64 x:
+//
+//   FP32 : values stored as FP32 (4 B), x rounded to FP32 once per call,
+//          FP32 products and per-lane FP32 accumulation; the lane partials
+//          are converted to FP64 and the VW-lane reduction and the long-row
+//          chunk fix-up run in FP64.
+//   BF16 : values stored as BF16 (2 B) after scaling each row by a power of
+//          two (row exponent stored as int8), FP32 products/accumulation, the
+//          scale is applied exactly in FP64 after the FP64 lane reduction.
+//   DF32 : values stored as FP64 (8 B), split in-kernel into FP32 (hi, lo)
+//          pairs, x split once per call; Dekker products and TwoSum
+//          accumulation in FP32 (double-float), FP64 reductions — FP64-level
+//          accuracy on the FP32 pipe.  An x outside the split range raises a
+//          flag: the DF32 launch then returns at once and a guard launch of
+//          the FP64 sliced kernel computes the call.
+//
+// x conversion kernels: f64 -> f32 with round-to-nearest-even written from
+// the IEEE-754 definition in integer arithmetic (no FP64 instructions: the
+// FP64 pipe of GB300 converts at about 0.28 G/s per SM group), and the
+// truncation split f64 -> (hi, lo) used by DF32.
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdint>
+
+#include "common.h"
+#include "sliced.h"
+#include "vnec_gb300.h"
+
+namespace vnec {
+namespace {
+
+constexpr unsigned kFull = 0xffffffffu;
+constexpr int kWarps = 8;
+
+// Round-to-nearest-even FP64 -> FP32 from the bit patterns (IEEE 754:
+// overflow to infinity, gradual underflow to subnormals, NaN stays NaN).
+__device__ __forceinline__ float f64_to_f32_rne(double v) {
+  const unsigned long long b = static_cast<unsigned long long>(__double_as_longlong(v));
+  const unsigned sign = static_cast<unsigned>(b >> 63) << 31;
+  const int e = static_cast<int>((b >> 52) & 0x7ff);
+  const unsigned long long m = b & 0xFFFFFFFFFFFFFull;
+  if (e == 0x7ff) return __uint_as_float(sign | 0x7f800000u | (m ? 0x00400000u : 0u));
+  const int E = e - 1023;
+  if (E > 127) return __uint_as_float(sign | 0x7f800000u);
+  if (e == 0) return __uint_as_float(sign);  // FP64 subnormals are far below FP32's range
+  unsigned long long M = m | (1ull << 52);   // 53-bit significand
+  int shift;                                 // bits of M dropped
+  unsigned expo;
+  if (E >= -126) {
+    shift = 29;
+    expo = static_cast<unsigned>(E + 127);
+  } else {
+    shift = 29 + (-126 - E);
+    expo = 0;
+    if (shift > 54) return __uint_as_float(sign);  // below half of the smallest subnormal
+  }
+  unsigned long long q = M >> shift;
+  const unsigned long long rem = M & ((1ull << shift) - 1);
+  const unsigned long long half = 1ull << (shift - 1);
+  if (rem > half || (rem == half && (q & 1))) ++q;
+  unsigned bits;
+  if (expo == 0) {
+    bits = static_cast<unsigned>(q);  // subnormal; a carry into bit 23 yields the smallest normal
+  } else {
+    if (q == (1ull << 24)) {  // rounding carried into a new binade
+      q >>= 1;
+      ++expo;
+      if (expo >= 255) return __uint_as_float(sign | 0x7f800000u);
+    }
+    bits = (expo << 23) | (static_cast<unsigned>(q) & 0x7FFFFFu);
+  }
+  return __uint_as_float(sign | bits);
+}
+
+// Truncation split of a double into hi + lo floats; false when a nonzero v
+// lies outside [2^-40, 2^41) (both halves and their products must stay
+// normal FP32 numbers).
+__device__ __forceinline__ bool split_df(double v, float& hi, float& lo) {
+  const unsigned long long b = static_cast<unsigned long long>(__double_as_longlong(v));
+  const unsigned sign = static_cast<unsigned>(b >> 63) << 31;
+  const int e = static_cast<int>((b >> 52) & 0x7ff);
+  const unsigned long long m = b & 0xFFFFFFFFFFFFFull;
+  if (e == 0 && m == 0) {
+    hi = 0.0f;
+    lo = 0.0f;
+    return true;
+  }
+  const int E = e - 1023;
+  const bool ok = (E >= -40) && (E <= 40);
+  hi = __uint_as_float(sign | (static_cast<unsigned>(E + 127) << 23) | static_cast<unsigned>(m >> 29));
+  const unsigned rem = static_cast<unsigned>(m & 0x1FFFFFFFull);
+  const int msb = 31 - __clz(rem | 1u);
+  const unsigned mant = msb > 23 ? (rem >> (msb - 23)) : (rem << (23 - msb));
+  lo = rem ? __uint_as_float(sign | (static_cast<unsigned>(E - 52 + msb + 127) << 23) | (mant & 0x7FFFFFu)) : 0.0f;
+  return ok;
+}
+
+}  // namespace
+
+// Outside the anonymous namespace: also launched by SpB_VNEC_f64_to_f32_ext.
+__global__ void x_to_f32_kernel(const double* __restrict__ x, float* __restrict__ x32, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    x32[i] = f64_to_f32_rne(x[i]);
+}
+namespace {
+
+__global__ void x_split_kernel(const double* __restrict__ x, float2* __restrict__ xs, long long n, int* flag) {
+  bool bad = false;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    float h, l;
+    bad |= !split_df(x[i], h, l);
+    xs[i] = make_float2(h, l);
+  }
+  if (__syncthreads_or(bad) && threadIdx.x == 0) atomicExch(flag, 1);
+}
+
+struct DF {
+  float s, c;
+};
+
+struct CodecF32 {
+  using Val = float;
+  using Acc = float;
+  __device__ static Acc zero() { return 0.0f; }
+  __device__ static Acc mac(Acc a, Val v, const void* xs, int c) {
+    return fmaf(v, __ldg(static_cast<const float*>(xs) + c), a);
+  }
+  __device__ static double to_f64(Acc a) { return static_cast<double>(a); }
+};
+
+struct CodecBF16 {
+  using Val = unsigned short;
+  using Acc = float;
+  __device__ static Acc zero() { return 0.0f; }
+  __device__ static Acc mac(Acc a, Val v, const void* xs, int c) {
+    return fmaf(__uint_as_float(static_cast<unsigned>(v) << 16), __ldg(static_cast<const float*>(xs) + c), a);
+  }
+  __device__ static double to_f64(Acc a) { return static_cast<double>(a); }
+};
+
+struct CodecDF32 {
+  using Val = double;
+  using Acc = DF;
+  __device__ static Acc zero() { return DF{0.0f, 0.0f}; }
+  __device__ static Acc mac(Acc acc, Val a, const void* xs, int c) {
+    float ah, al;
+    split_df(a, ah, al);  // A's range was checked when the plan was built
+    const float2 x = __ldg(static_cast<const float2*>(xs) + c);
+    const float p = __fmul_rn(ah, x.x);
+    const float e = fmaf(ah, x.x, -p);              // ah*xh = p + e exactly
+    const float q = fmaf(ah, x.y, fmaf(al, x.x, e));
+    const float t = __fadd_rn(acc.s, p);            // TwoSum(acc.s, p)
+    const float bb = __fsub_rn(t, acc.s);
+    const float r = __fadd_rn(__fsub_rn(acc.s, __fsub_rn(t, bb)), __fsub_rn(p, bb));
+    return DF{t, __fadd_rn(acc.c, __fadd_rn(r, q))};
+  }
+  __device__ static double to_f64(Acc a) { return static_cast<double>(a.s) + static_cast<double>(a.c); }
+};
+
+template <typename T> __device__ __forceinline__ T ld_stream(const T* p) { return __ldcs(p); }
+template <> __device__ __forceinline__ unsigned short ld_stream<unsigned short>(const unsigned short* p) {
+  return __ldcs(p);
+}
+
+__device__ __forceinline__ double pow2(int e) {
+  return __longlong_as_double(static_cast<long long>(e + 1023) << 52);
+}
+
+template <class C, int U>
+__global__ void __launch_bounds__(kWarps * 32)
+sliced_mixed_kernel(const SlicedTask* __restrict__ tasks, long long num_tasks, const typename C::Val* __restrict__ val,
+                    const int32_t* __restrict__ col, const int32_t* __restrict__ rowid, const void* __restrict__ xs,
+                    double* __restrict__ y, double* __restrict__ chunk_sum, const signed char* __restrict__ row_scale,
+                    const signed char* __restrict__ chunk_scale, const int* __restrict__ flag) {
+  if (flag && *reinterpret_cast<const volatile int*>(flag)) return;  // DF32: x out of range, guard launch computes
+  const long long w = ((long long)blockIdx.x * kWarps) + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  if (w >= num_tasks) return;
+  const int4 raw = __ldg(reinterpret_cast<const int4*>(tasks) + w);
+  const int base = raw.x, row_base = raw.y, steps = raw.z, meta = raw.w;
+  const int kind = meta & 15, vwl = (meta >> 4) & 15, nrows = meta >> 8;
+  if (kind == kSlicedZero) {
+    if (lane < nrows) y[rowid[row_base + lane]] = 0.0;
+    return;
+  }
+  const typename C::Val* vp = val + base + lane;
+  const int32_t* cp = col + base + lane;
+  typename C::Acc acc = C::zero();
+  int k = 0;
+  for (; k + U <= steps; k += U) {
+    int c[U];
+    typename C::Val v[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      c[u] = __ldcs(cp + (k + u) * 32);
+      v[u] = ld_stream(vp + (k + u) * 32);
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u) acc = C::mac(acc, v[u], xs, c[u]);
+  }
+  for (; k < steps; ++k) acc = C::mac(acc, ld_stream(vp + k * 32), xs, __ldcs(cp + k * 32));
+  double s = C::to_f64(acc);
+  for (int off = (1 << vwl) >> 1; off > 0; off >>= 1) s += __shfl_xor_sync(kFull, s, off);
+  if (kind == kSlicedChunk) {
+    if (lane == 0) chunk_sum[row_base] = chunk_scale ? s * pow2(chunk_scale[row_base]) : s;
+  } else {
+    const int g = lane >> vwl;
+    if ((lane & ((1 << vwl) - 1)) == 0 && g < nrows)
+      y[rowid[row_base + g]] = row_scale ? s * pow2(row_scale[row_base + g]) : s;
+  }
+}
+
+__global__ void long_fixup_f64(const int32_t* __restrict__ long_row, const int32_t* __restrict__ long_first,
+                               long long num_long, const double* __restrict__ chunk_sum, double* __restrict__ y,
+                               int* flag) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i == 0 && flag) *flag = 0;  // consumed: reset for the next call
+  if (i >= num_long) return;
+  double s = 0.0;
+  for (int c = long_first[i]; c < long_first[i + 1]; ++c) s += chunk_sum[c];
+  y[long_row[i]] = s;
+}
+
+__global__ void reset_flag(int* flag) { *flag = 0; }
+
+template <class C>
+bool launch_mixed(const SlicedMatrix& m, const SlicedMixed& mx, const void* xs, double* y, cudaStream_t s,
+                  const int* flag) {
+  const long long grid = (m.num_tasks + kWarps - 1) / kWarps;
+  if (grid > 0x7fffffffLL) {
+    set_error("sliced: too many tasks for one launch");
+    return false;
+  }
+  sliced_mixed_kernel<C, 8><<<(unsigned)grid, kWarps * 32, 0, s>>>(
+      m.tasks, m.num_tasks, static_cast<const typename C::Val*>(m.val), m.col, m.rowid, xs, y,
+      static_cast<double*>(m.chunk_sum), mx.row_scale, mx.chunk_scale, flag);
+  return VNEC_CUDA(cudaGetLastError());
+}
+
+}  // namespace
+
+bool sliced_mixed_spmv(const SlicedMatrix& m, const SlicedMixed& mx, const double* x, double* y, cudaStream_t s,
+                       cudaEvent_t* ev) {
+  if (ev && !VNEC_CUDA(cudaEventRecord(ev[0], s))) return false;
+  const int tb = 256;
+  const long long nx = m.n_cols;
+  const int xg = (int)std::min<long long>((nx + tb - 1) / tb, 152LL * 16);
+  int* flag = nullptr;
+  if (nx > 0) {
+    if (mx.precision == kPrecDF32) {
+      x_split_kernel<<<xg, tb, 0, s>>>(x, static_cast<float2*>(mx.xbuf), nx, mx.flag);
+      flag = mx.flag;
+    } else {
+      x_to_f32_kernel<<<xg, tb, 0, s>>>(x, static_cast<float*>(mx.xbuf), nx);
+    }
+    if (!VNEC_CUDA(cudaGetLastError())) return false;
+  }
+  if (m.num_tasks > 0) {
+    bool ok = false;
+    switch (mx.precision) {
+      case kPrecFP32: ok = launch_mixed<CodecF32>(m, mx, mx.xbuf, y, s, nullptr); break;
+      case kPrecBF16: ok = launch_mixed<CodecBF16>(m, mx, mx.xbuf, y, s, nullptr); break;
+      case kPrecDF32: ok = launch_mixed<CodecDF32>(m, mx, mx.xbuf, y, s, flag); break;
+      default: set_error("sliced: unknown precision form"); return false;
+    }
+    if (!ok) return false;
+  }
+  if (ev && !VNEC_CUDA(cudaEventRecord(ev[1], s))) return false;
+  if (mx.precision == kPrecDF32 && m.num_tasks > 0) {
+    // Guard: the FP64 sliced kernel, which returns at once unless the flag is set.
+    if (!sliced_guard_f64(m, x, y, mx.flag, s)) return false;
+  }
+  if (m.num_long > 0) {
+    const int b = 128;
+    long_fixup_f64<<<(unsigned)((m.num_long + b - 1) / b), b, 0, s>>>(
+        m.long_row, m.long_first, m.num_long, static_cast<const double*>(m.chunk_sum), y,
+        mx.precision == kPrecDF32 ? mx.flag : nullptr);
+    if (!VNEC_CUDA(cudaGetLastError())) return false;
+  } else if (mx.precision == kPrecDF32) {
+    reset_flag<<<1, 1, 0, s>>>(mx.flag);
+    if (!VNEC_CUDA(cudaGetLastError())) return false;
+  }
+  if (ev && !VNEC_CUDA(cudaEventRecord(ev[2], s))) return false;
+  return true;
+}
+
+}  // namespace vnec
+
+extern "C" SpB_Info SpB_VNEC_f64_to_f32_ext(const double* d_in, float* d_out, int64_t n, void* stream) {
+  vnec::clear_error();
+  if (n < 0 || (n > 0 && (!d_in || !d_out))) {
+    vnec::set_error("SpB_VNEC_f64_to_f32_ext: invalid arguments");
+    return SpB_FAILURE;
+  }
+  if (n == 0) return SpB_SUCCESS;
+  const int tb = 256;
+  const int grid = (int)std::min<long long>((n + tb - 1) / tb, 152LL * 16);
+  vnec::x_to_f32_kernel<<<grid, tb, 0, static_cast<cudaStream_t>(stream)>>>(d_in, d_out, n);
+  return VNEC_CUDA(cudaGetLastError()) ? SpB_SUCCESS : SpB_FAILURE;
+}

@@ -2,7 +2,9 @@
 // dense-block format built on the same warp-task layout (VNEC-D counterpart).
 
 #include <algorithm>
+#include <cmath>
 #include <cstring>
+#include <limits>
 
 #include "host.h"
 #include "sliced.h"
@@ -12,12 +14,16 @@ namespace {
 
 struct SlicedPlan final : Plan {
   SlicedMatrix m;
-  DeviceBuffer tasks, val, col, rowid, long_row, long_first, chunk_sum;
+  SlicedMixed mx;  // precision form (FP64 = plain)
+  DeviceBuffer tasks, val, col, rowid, long_row, long_first, chunk_sum, xbuf, flag, row_scale, chunk_scale;
   SlicedParams prm;
   int64_t blocks = 0;  // dense-block plans: number of blocks of 4
   explicit SlicedPlan(PlanKind k) : Plan(k) {}
   bool run(const void* d_x, void* d_y, cudaStream_t s) override {
     if (profiling && !ensure_events()) return false;
+    if (mx.precision != kPrecFP64)
+      return sliced_mixed_spmv(m, mx, static_cast<const double*>(d_x), static_cast<double*>(d_y), s,
+                               profiling ? events : nullptr);
     return sliced_spmv(m, type == SpB_FP64, d_x, d_y, s, profiling ? events : nullptr);
   }
   int kernel_ms(float* ms, int cap) const override {
@@ -27,14 +33,21 @@ struct SlicedPlan final : Plan {
     cudaEventElapsedTime(&ms[1], events[1], events[2]);
     return 2;
   }
-  int launches_per_call() const override { return n_rows > 0 ? sliced_launches(m) : 0; }
+  int launches_per_call() const override {
+    if (n_rows == 0) return 0;
+    return mx.precision != kPrecFP64 ? sliced_mixed_launches(m, mx.precision) : sliced_launches(m);
+  }
   int64_t device_bytes() const override {
     return (int64_t)(tasks.bytes + val.bytes + col.bytes + rowid.bytes + long_row.bytes + long_first.bytes +
-                     chunk_sum.bytes + dx.bytes + dy.bytes);
+                     chunk_sum.bytes + xbuf.bytes + flag.bytes + row_scale.bytes + chunk_scale.bytes + dx.bytes +
+                     dy.bytes);
   }
   int64_t algorithmic_bytes() const override {
-    const int64_t vb = type == SpB_FP64 ? 8 : 4;
-    return nnz * (vb + 4) + (n_rows + 1) * 4 + n_cols * vb + n_rows * vb;
+    // Stored value size of the form; x and y stay in the matrix's type.
+    const int64_t io = type == SpB_FP64 ? 8 : 4;
+    const int64_t sv = mx.precision == kPrecFP32 ? 4 : mx.precision == kPrecBF16 ? 2 : io;
+    const int64_t scale = mx.precision == kPrecBF16 ? n_rows : 0;
+    return nnz * (sv + 4) + (n_rows + 1) * 4 + scale + n_cols * io + n_rows * io;
   }
   void describe(SpB_VNEC_info_ext* info) const override {
     info->kernel = kind == PlanKind::kWindowDense ? SpB_VNEC_KERNEL_D : SpB_VNEC_KERNEL_S;
@@ -42,6 +55,7 @@ struct SlicedPlan final : Plan {
     info->items_per_thread = prm.max_steps;
     info->num_tiles = m.num_tasks;
     info->blocks = blocks;
+    info->precision = mx.precision;
   }
 };
 
@@ -54,24 +68,75 @@ SlicedParams params_from(const SpB_VNEC_options_ext* opts) {
   return prm;
 }
 
-// Uploads a built host layout into a plan.
-std::unique_ptr<Plan> upload(std::unique_ptr<SlicedPlan> p, SlicedHost* h, int vb, const SpB_VNEC_options_ext* opts) {
+// FP64 -> BF16: round to nearest even applied to the FP32 rounding of the
+// value.  This double rounding can differ from a direct FP64 -> BF16 rounding
+// by one BF16 unit in rare ties; the stored value stays within 2^-8 relative.
+uint16_t to_bf16(double v) {
+  const float f = static_cast<float>(v);
+  uint32_t b;
+  std::memcpy(&b, &f, 4);
+  if ((b & 0x7f800000u) == 0x7f800000u) return static_cast<uint16_t>((b >> 16) | ((b & 0xffff) ? 0x40 : 0));
+  b += 0x7fffu + ((b >> 16) & 1u);
+  return static_cast<uint16_t>(b >> 16);
+}
+
+// Uploads a built host layout into a plan.  `row_exp` (BF16 form): the
+// power-of-two exponent each row was scaled by.
+std::unique_ptr<Plan> upload(std::unique_ptr<SlicedPlan> p, SlicedHost* h, int vb, const SpB_VNEC_options_ext* opts,
+                             const std::vector<signed char>* row_exp = nullptr) {
   std::unique_ptr<SlicedHost, void (*)(SlicedHost*)> guard(h, sliced_free);
   SlicedHostView hv = sliced_view(h);
-  const size_t eb = (size_t)vb * hv.vpe;
   const size_t pad = 64;
+  const int prec = p->mx.precision;
+  // Stored values: FP64/FP32 as built, or converted for the FP32 / BF16 forms.
+  std::vector<unsigned char> conv;
+  const void* vals = hv.val;
+  size_t evb = (size_t)vb;
+  if (prec == kPrecFP32 || prec == kPrecBF16) {
+    const double* src = static_cast<const double*>(hv.val);
+    const int64_t ne = hv.entries + (int64_t)pad;
+    evb = prec == kPrecFP32 ? 4 : 2;
+    conv.resize((size_t)ne * evb);
+    if (prec == kPrecFP32) {
+      float* d = reinterpret_cast<float*>(conv.data());
+#pragma omp parallel for schedule(static)
+      for (int64_t i = 0; i < ne; ++i) d[i] = static_cast<float>(src[i]);
+    } else {
+      uint16_t* d = reinterpret_cast<uint16_t*>(conv.data());
+#pragma omp parallel for schedule(static)
+      for (int64_t i = 0; i < ne; ++i) d[i] = to_bf16(src[i]);
+    }
+    vals = conv.data();
+  }
+  const size_t eb = evb * hv.vpe;
   auto up = [](DeviceBuffer& b, const void* src, size_t bytes, size_t alloc) {
     if (!b.alloc(std::max(alloc, bytes))) return false;
     return bytes == 0 || VNEC_CUDA(cudaMemcpy(b.ptr, src, bytes, cudaMemcpyHostToDevice));
   };
   if (!up(p->tasks, hv.tasks, sizeof(SlicedTask) * hv.num_tasks, sizeof(SlicedTask) * hv.num_tasks) ||
-      !up(p->val, hv.val, eb * (hv.entries + pad), 0) ||
+      !up(p->val, vals, eb * (hv.entries + pad), 0) ||
       !up(p->col, hv.col, 4 * (size_t)(hv.entries + pad), 0) ||
       !up(p->rowid, hv.rowid, 4 * (size_t)hv.n_rowid, 4 * (size_t)hv.n_rowid + 64) ||
       !up(p->long_row, hv.long_row, 4 * (size_t)hv.num_long, 4 * (size_t)hv.num_long + 64) ||
       !up(p->long_first, hv.long_first, 4 * (size_t)(hv.num_long + 1), 0) ||
       !p->chunk_sum.alloc((size_t)vb * (hv.num_chunks + 1)))
     return nullptr;
+  if (prec != kPrecFP64) {
+    if (!p->xbuf.alloc((size_t)std::max<int64_t>(p->n_cols, 1) * (prec == kPrecDF32 ? 8 : 4)) || !p->flag.alloc(16) ||
+        !VNEC_CUDA(cudaMemset(p->flag.ptr, 0, 16)))
+      return nullptr;
+    p->mx.xbuf = p->xbuf.ptr;
+    p->mx.flag = p->flag.as<int>();
+  }
+  if (prec == kPrecBF16) {
+    std::vector<signed char> rs((size_t)std::max<int64_t>(hv.n_rowid, 1)), cs((size_t)std::max<int64_t>(hv.num_chunks, 1));
+    for (int64_t k = 0; k < hv.n_rowid; ++k) rs[(size_t)k] = (*row_exp)[(size_t)hv.rowid[k]];
+    for (int64_t i = 0; i < hv.num_long; ++i)
+      for (int32_t c = hv.long_first[i]; c < hv.long_first[i + 1]; ++c) cs[(size_t)c] = (*row_exp)[(size_t)hv.long_row[i]];
+    if (!up(p->row_scale, rs.data(), rs.size(), 0) || !up(p->chunk_scale, cs.data(), cs.size(), 0)) return nullptr;
+    p->mx.row_scale = p->row_scale.as<signed char>();
+    p->mx.chunk_scale = p->chunk_scale.as<signed char>();
+  }
   SlicedMatrix& m = p->m;
   m.n_rows = p->n_rows;
   m.n_cols = p->n_cols;
@@ -103,13 +168,67 @@ std::unique_ptr<Plan> build_sliced(const CsrView& v, const SpB_VNEC_options_ext*
   p->nnz = v.nnz;
   cudaGetDevice(&p->device);
   p->prm = params_from(opts);
+  const int prec = opts ? opts->precision : kPrecFP64;
+  if (prec < kPrecFP64 || prec > kPrecDF32) {
+    set_error("unknown precision form");
+    return nullptr;
+  }
+  if (prec != kPrecFP64 && v.type != SpB_FP64) {
+    set_error("precision forms apply to FP64 matrices");
+    return nullptr;
+  }
+  p->mx.precision = prec;
   const int vb = (int)v.value_bytes();
-  SlicedHost* h = sliced_build(v.n_rows, v.n_cols, v.ptr, v.ptr64, v.idx, v.idx64, v.val, vb, p->prm);
+  const double* a = static_cast<const double*>(v.val);
+  int bad = 0;
+  std::vector<signed char> row_exp;
+  std::vector<double> scaled;
+  const void* src_val = v.val;
+  if (prec == kPrecFP32) {
+#pragma omp parallel for schedule(static) reduction(| : bad)
+    for (int64_t q = 0; q < v.nnz; ++q)
+      if (!(std::fabs(a[q]) <= (double)std::numeric_limits<float>::max())) bad = 1;
+    if (bad) {
+      set_error("FP32 form: a matrix value is not finite in FP32");
+      return nullptr;
+    }
+  } else if (prec == kPrecDF32) {
+#pragma omp parallel for schedule(static) reduction(| : bad)
+    for (int64_t q = 0; q < v.nnz; ++q) {
+      int e = 0;
+      if (a[q] != 0.0 && (!std::isfinite(a[q]) || (std::frexp(a[q], &e), e - 1 < -40 || e - 1 > 40))) bad = 1;
+    }
+    if (bad) {
+      set_error("DF32 form: a matrix value lies outside [2^-40, 2^41)");
+      return nullptr;
+    }
+  } else if (prec == kPrecBF16) {
+    // Row scale 2^-e with e the exponent of the row's largest |value| (so the
+    // scaled values lie in (-1, 1)), stored as int8.
+    row_exp.assign((size_t)v.n_rows, 0);
+    scaled.assign((size_t)std::max<int64_t>(v.nnz, 1), 0.0);
+#pragma omp parallel for schedule(static) reduction(| : bad)
+    for (int64_t r = 0; r < v.n_rows; ++r) {
+      double mx = 0.0;
+      for (int64_t q = v.row_begin(r); q < v.row_begin(r + 1); ++q) mx = std::max(mx, std::fabs(a[q]));
+      int e = 0;
+      if (mx > 0.0) std::frexp(mx, &e);
+      if (!std::isfinite(mx) || e < -120 || e > 120) bad = 1;
+      row_exp[(size_t)r] = (signed char)std::max(-120, std::min(120, e));
+      for (int64_t q = v.row_begin(r); q < v.row_begin(r + 1); ++q) scaled[(size_t)q] = std::ldexp(a[q], -e);
+    }
+    if (bad) {
+      set_error("BF16 form: a row's magnitude is outside 2^[-120, 120] or not finite");
+      return nullptr;
+    }
+    src_val = scaled.data();
+  }
+  SlicedHost* h = sliced_build(v.n_rows, v.n_cols, v.ptr, v.ptr64, v.idx, v.idx64, src_val, vb, p->prm);
   if (!h) {
     set_error("sliced format: more than 2^31 entries or row slots");
     return nullptr;
   }
-  return upload(std::move(p), h, vb, opts);
+  return upload(std::move(p), h, vb, opts, prec == kPrecBF16 ? &row_exp : nullptr);
 }
 
 // Dense-block format (VNEC-D counterpart, spmv_vnec_D_for_mxv.c:242-398):
