@@ -105,7 +105,8 @@ typedef enum {
   SpB_VNEC_KERNEL_AUTO = 0,
   SpB_VNEC_KERNEL_L = 1, /* merge-path CSR */
   SpB_VNEC_KERNEL_D = 2, /* windowed dense blocks */
-  SpB_VNEC_KERNEL_S = 3  /* windowed sliced rows */
+  SpB_VNEC_KERNEL_S = 3, /* windowed sliced rows */
+  SpB_VNEC_KERNEL_BATCH = 4 /* batched multi-right-hand-side plans (SpB_VNEC_batch_plan_ext) */
 } SpB_VNEC_kernel_ext;
 
 /* Arithmetic of the FP64 merge-path kernel. */
@@ -179,8 +180,10 @@ typedef struct {
   int pipeline_stages;     /* 0 for the unpipelined kernel */
   int arithmetic;          /* SpB_VNEC_arith_ext in use */
   int64_t blocks;          /* dense-block plans: blocks of 4 columns (fill = nnz / (4 * blocks)) */
-  int precision;           /* SpB_VNEC_precision_ext of a sliced plan */
-  int reserved[3];
+  int precision;           /* SpB_VNEC_precision_ext of a sliced or batch plan */
+  int rhs;                 /* right-hand sides k (1 for single-vector plans) */
+  int lanes;               /* batch plans: lanes per row (items_per_thread = k / lanes per lane) */
+  int long_row_len;        /* sliced and batch plans: rows longer than this are chunked */
 } SpB_VNEC_info_ext;
 
 /* Device-side error status of the plan's last calls: waits for the plan's
@@ -216,6 +219,51 @@ SpB_Info SpB_mxv_csr_noalloc_ext(int64_t n_rows, int64_t n_cols, int64_t nnz, co
                                  void *stream);
 
 SpB_Info SpB_VNEC_plan_info_ext(const void *plan, SpB_VNEC_info_ext *info);
+
+/* Batched multi-right-hand-side mxv (no counterpart in the reference, whose
+ * SpB_mxv multiplies one matrix by one vector).
+ *
+ * Y_m := A_m X_m for n_mats independent FP64 CSR matrices of any sizes and k
+ * right-hand sides (k = 1, 2, 4, 8, 16 or 32).  X_m is dense row-major
+ * n_cols[m] x k, Y_m is n_rows[m] x k.  A plan's x and y are the
+ * concatenations of the X_m and Y_m in matrix order (offsets from
+ * SpB_VNEC_batch_offsets_ext, in rows of k values), so one
+ * SpB_mxv_device_ext / SpB_mxv_host_ext call runs the whole batch: one
+ * persistent kernel (the FP32 form adds one launch that rounds X), replayed
+ * from a CUDA graph captured on the first call with a given (x, y) pair.
+ * Device x and y must be 16-byte aligned when k / lanes >= 2.  Calls on one
+ * batch plan must not overlap on the GPU (they share the plan's long-row
+ * scratch). */
+typedef struct {
+  int precision;       /* SpB_VNEC_PREC_FP64 (0) or SpB_VNEC_PREC_FP32 */
+  int lanes;           /* lanes per row (divides 32 and k, k / lanes in {1,2,4,8}); 0: tuned or default */
+  int long_row_len;    /* rows longer than this are cut into chunks; 0: tuned or 1024 */
+  int chunk;           /* entries per chunk; 0: long_row_len */
+  int warps_per_block; /* 4 or 8; 0: tuned or 8 */
+  int autotune;        /* 1: time candidate layouts on a sample of the batch and keep the fastest */
+  int no_graph;        /* 1: launch the kernels directly on each call */
+  int window_rows;     /* rows sorted by length within windows of this size (0: 65536) */
+  int reserved[8];
+} SpB_VNEC_batch_options_ext;
+
+/* Plan from host CSR arrays per matrix: int64 row offsets (n_rows[m] + 1),
+ * int32 columns, FP64 values.  The arrays are copied.  NULL on failure. */
+void *SpB_VNEC_batch_plan_ext(int n_mats, const int64_t *n_rows, const int64_t *n_cols,
+                              const int64_t *const *row_ptr, const int32_t *const *col, const double *const *val,
+                              int k, const SpB_VNEC_batch_options_ext *opts);
+
+/* Plan from reference FP64 SpB_Matrix objects. */
+void *SpB_VNEC_batch_plan_matrices_ext(int n_mats, const SpB_Matrix *A, int k,
+                                       const SpB_VNEC_batch_options_ext *opts);
+
+/* Row and column offsets of each matrix in the concatenation (n_mats + 1
+ * entries each, in rows; multiply by k for element offsets). */
+SpB_Info SpB_VNEC_batch_offsets_ext(const void *plan, int64_t *row_offset, int64_t *col_offset);
+
+/* Autotuner result of a batch plan: candidates timed (0 if not tuned) and,
+ * per candidate, {lanes, long_row_len, warps_per_block} and its median
+ * milliseconds on the sample (up to `cap` entries); *best = chosen index. */
+int SpB_VNEC_batch_tuning_ext(const void *plan, int *configs, float *ms, int cap, int *best);
 
 /* Per-kernel timing: when enabled, each SpMV of the plan records CUDA events
  * around each of its kernels on the launching stream;

@@ -48,6 +48,7 @@ def lib() -> C.CDLL:
         L.orc_spmv_serial_f64.argtypes = [_i64] + [_vp] * 5
         L.orc_spmv_serial_f32.argtypes = [_i64] + [_vp] * 5
         L.orc_spmv_neumaier_f64.argtypes = [_i64] + [_vp] * 6
+        L.orc_spmm_neumaier_f64.argtypes = [_i64, _vp, _vp, _vp, C.c_int, _vp, _vp, _vp]
         L.orc_spmv_L_f64.argtypes = [C.c_int, _i64, _i64] + [_vp] * 5
         L.orc_spmv_L_f32.argtypes = [C.c_int, C.c_int, _i64, _i64] + [_vp] * 5
         for f in ("orc_spmv_D_f64", "orc_spmv_S_f64", "orc_spmv_D_f32", "orc_spmv_S_f32"):
@@ -111,6 +112,19 @@ def spmv_neumaier(m, x) -> tuple[np.ndarray, np.ndarray]:
     cond = np.zeros(m.n_rows)
     lib().orc_spmv_neumaier_f64(m.n_rows, _p(rp), _p(ci), _p(v), _p(xx), _p(y), _p(cond))
     return y, cond
+
+
+def spmm_neumaier(m, X) -> tuple[np.ndarray, np.ndarray]:
+    """Compensated FP64 Y = A X for row-major X (n_cols x k) and the
+    conditioning sums, both n_rows x k (the batched path's checker)."""
+    rp, ci = _csr(m)
+    v = np.ascontiguousarray(m.val, dtype=np.float64)
+    X = np.ascontiguousarray(X, dtype=np.float64).reshape(m.n_cols, -1)
+    k = X.shape[1]
+    Y = np.zeros((m.n_rows, k))
+    cond = np.zeros((m.n_rows, k))
+    lib().orc_spmm_neumaier_f64(m.n_rows, _p(rp), _p(ci), _p(v), k, _p(X), _p(Y), _p(cond))
+    return Y, cond
 
 
 def spmv_vnec(variant: str, m, x, dtype=np.float64, build=X86) -> np.ndarray:

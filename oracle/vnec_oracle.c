@@ -216,6 +216,36 @@ void orc_spmv_neumaier_f64(i64 n_rows, const i64 *row_ptr, const int32_t *col, c
   }
 }
 
+/* Multi-right-hand-side form of orc_spmv_neumaier_f64 for the batched path
+ * (which has no reference counterpart: the reference's SpB_mxv takes one
+ * vector).  X is row-major n_cols x k, Y and cond row-major n_rows x k;
+ * column j of Y is the compensated FP64 product of the matrix with column j
+ * of X, and cond its sum_p |a_p x_p|. */
+void orc_spmm_neumaier_f64(i64 n_rows, const i64 *row_ptr, const int32_t *col, const double *val, int k,
+                           const double *X, double *Y, double *cond) {
+#pragma omp parallel for schedule(dynamic, 64)
+  for (i64 i = 0; i < n_rows; ++i) {
+    for (int j = 0; j < k; ++j) {
+      double s = 0.0, c = 0.0, a = 0.0;
+      for (i64 p = row_ptr[i]; p < row_ptr[i + 1]; ++p) {
+        const double xv = X[(i64)col[p] * k + j];
+        double prod = val[p] * xv;
+        double perr = fma(val[p], xv, -prod);
+        double t = s + prod;
+        if (fabs(s) >= fabs(prod))
+          c += (s - t) + prod;
+        else
+          c += (prod - t) + s;
+        s = t;
+        c += perr;
+        a += fabs(prod);
+      }
+      Y[i * k + j] = s + c;
+      if (cond) cond[i * k + j] = a;
+    }
+  }
+}
+
 /* ------------------------------------------------------------------------ */
 /* VNEC-L: merge-path CSR                                                    */
 /* ------------------------------------------------------------------------ */

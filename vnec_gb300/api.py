@@ -25,7 +25,7 @@ SpB_FP32, SpB_FP64 = 10, 11
 SpB_DENSE = 0
 SpB_CSC, SpB_CSR = 0, 1
 SpB_VNEC_D, SpB_VNEC_S = 0, 1
-KERNEL_AUTO, KERNEL_L, KERNEL_D, KERNEL_S = 0, 1, 2, 3
+KERNEL_AUTO, KERNEL_L, KERNEL_D, KERNEL_S, KERNEL_BATCH = 0, 1, 2, 3, 4
 ARITH_AUTO, ARITH_FP64, ARITH_DF32 = 0, 1, 2
 PREC_FP64, PREC_FP32, PREC_BF16, PREC_DF32 = 0, 1, 2, 3
 
@@ -72,7 +72,16 @@ class Info(C.Structure):
                 ("nnz", C.c_int64), ("device_bytes", C.c_int64), ("algorithmic_bytes", C.c_int64),
                 ("launches_per_call", C.c_int), ("threads_per_block", C.c_int), ("items_per_thread", C.c_int),
                 ("num_tiles", C.c_int64), ("pipeline_stages", C.c_int), ("arithmetic", C.c_int),
-                ("blocks", C.c_int64), ("precision", C.c_int), ("reserved", C.c_int * 3)]
+                ("blocks", C.c_int64), ("precision", C.c_int), ("rhs", C.c_int), ("lanes", C.c_int),
+                ("long_row_len", C.c_int)]
+
+
+class BatchOptions(C.Structure):
+    """SpB_VNEC_batch_options_ext."""
+
+    _fields_ = [("precision", C.c_int), ("lanes", C.c_int), ("long_row_len", C.c_int), ("chunk", C.c_int),
+                ("warps_per_block", C.c_int), ("autotune", C.c_int), ("no_graph", C.c_int),
+                ("window_rows", C.c_int), ("reserved", C.c_int * 8)]
 
 
 _vp = C.c_void_p
@@ -123,6 +132,14 @@ def lib() -> C.CDLL:
     L.SpB_VNEC_device_status_ext.restype = C.c_int
     L.SpB_VNEC_f64_to_f32_ext.argtypes = [_vp, _vp, C.c_int64, _vp]
     L.SpB_VNEC_f64_to_f32_ext.restype = C.c_int
+    L.SpB_VNEC_batch_plan_ext.argtypes = [C.c_int, _vp, _vp, _vp, _vp, _vp, C.c_int, C.POINTER(BatchOptions)]
+    L.SpB_VNEC_batch_plan_ext.restype = _vp
+    L.SpB_VNEC_batch_plan_matrices_ext.argtypes = [C.c_int, _vp, C.c_int, C.POINTER(BatchOptions)]
+    L.SpB_VNEC_batch_plan_matrices_ext.restype = _vp
+    L.SpB_VNEC_batch_offsets_ext.argtypes = [_vp, _vp, _vp]
+    L.SpB_VNEC_batch_offsets_ext.restype = C.c_int
+    L.SpB_VNEC_batch_tuning_ext.argtypes = [_vp, _vp, _vp, C.c_int, C.POINTER(C.c_int)]
+    L.SpB_VNEC_batch_tuning_ext.restype = C.c_int
     L._vnec_typed = True
     return L
 
@@ -361,3 +378,74 @@ class Plan:
             self.free()
         except Exception:
             pass
+
+
+def batch_options(precision: int = PREC_FP64, lanes: int = 0, long_row_len: int = 0, chunk: int = 0,
+                  warps_per_block: int = 0, autotune: bool = False, graph: bool = True,
+                  window_rows: int = 0) -> BatchOptions:
+    o = BatchOptions()
+    o.precision, o.lanes, o.long_row_len, o.chunk = precision, lanes, long_row_len, chunk
+    o.warps_per_block, o.autotune, o.no_graph, o.window_rows = warps_per_block, int(autotune), int(not graph), \
+        window_rows
+    return o
+
+
+class BatchPlan(Plan):
+    """Batched multi-right-hand-side plan: Y_m = A_m X_m for a list of FP64 CSR
+    matrices (objects with n_rows, n_cols, row_ptr, col, val) or Matrix objects,
+    with k right-hand sides; x / y of the calls are the row-major concatenations."""
+
+    def __init__(self, mats, k: int, *, opts: BatchOptions | None = None, **kw):  # noqa: D107
+        o = opts or batch_options(**kw)
+        L = lib()
+        n = len(mats)
+        if n and isinstance(mats[0], Matrix):
+            arr = (C.c_void_p * n)(*[m.handle for m in mats])
+            h = L.SpB_VNEC_batch_plan_matrices_ext(n, arr, k, C.byref(o))
+        else:
+            keep = []
+            nr = np.array([m.n_rows for m in mats], dtype=np.int64)
+            nc = np.array([m.n_cols for m in mats], dtype=np.int64)
+            rps, cis, vls = (C.c_void_p * n)(), (C.c_void_p * n)(), (C.c_void_p * n)()
+            for i, m in enumerate(mats):
+                rp = np.ascontiguousarray(m.row_ptr, dtype=np.int64)
+                ci = np.ascontiguousarray(m.col, dtype=np.int32)
+                vv = np.ascontiguousarray(m.val, dtype=np.float64)
+                keep += [rp, ci, vv]
+                rps[i], cis[i], vls[i] = rp.ctypes.data, ci.ctypes.data, vv.ctypes.data
+            h = L.SpB_VNEC_batch_plan_ext(n, nr.ctypes.data, nc.ctypes.data, rps, cis, vls, k, C.byref(o))
+        _check(bool(h), "batch plan")
+        self.h = h
+        self.type = SpB_FP64
+        self.dtype = np.float64
+        self.k = k
+        self.n_mats = n
+
+    def offsets(self) -> tuple[np.ndarray, np.ndarray]:
+        """Row and column offsets of each matrix (n_mats + 1 each, in rows of k values)."""
+        ro = np.zeros(self.n_mats + 1, dtype=np.int64)
+        co = np.zeros(self.n_mats + 1, dtype=np.int64)
+        _check(lib().SpB_VNEC_batch_offsets_ext(self.h, ro.ctypes.data, co.ctypes.data) == SpB_SUCCESS,
+               "batch_offsets")
+        return ro, co
+
+    def mxv_host(self, x: np.ndarray, y: np.ndarray | None = None) -> np.ndarray:
+        inf = self.info()
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        if x.size != inf.n_cols * self.k:
+            raise ValueError("x must hold n_cols * k values")
+        if y is None:
+            y = np.empty((inf.n_rows, self.k), dtype=np.float64)
+        _check(lib().SpB_mxv_host_ext(self.h, x.ctypes.data, y.ctypes.data) == SpB_SUCCESS, "SpB_mxv_host_ext")
+        return y
+
+    def tuning(self) -> tuple[list[tuple[int, int, int]], list[float], int]:
+        """Autotuner record: candidates (lanes, long_row_len, warps_per_block), median ms, chosen index."""
+        cap = 256
+        cfg = (C.c_int * (3 * cap))()
+        ms = (C.c_float * cap)()
+        best = C.c_int(-1)
+        n = lib().SpB_VNEC_batch_tuning_ext(self.h, cfg, ms, cap, C.byref(best))
+        _check(n >= 0, "batch_tuning")
+        n = min(n, cap)
+        return [(cfg[3 * i], cfg[3 * i + 1], cfg[3 * i + 2]) for i in range(n)], [ms[i] for i in range(n)], best.value

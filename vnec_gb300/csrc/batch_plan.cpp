@@ -1,0 +1,561 @@
+// Batch plans: the batched multi-right-hand-side layout (batch.h) in device
+// memory, the CUDA graph each call replays, and the autotuner that picks the
+// layout (lanes per row, long-row limit) and block size by timing candidates
+// on a sample of the batch.
+
+#include <omp.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "batch.h"
+#include "host.h"
+
+namespace vnec {
+namespace {
+
+struct BatchDev {
+  DeviceBuffer tasks, val, val32, col, rowid, long_row, long_first, chunk_long, chunk_sum, chunk_count, xbuf;
+  BatchMatrix m;
+  int64_t bytes() const {
+    return (int64_t)(tasks.bytes + val.bytes + val32.bytes + col.bytes + rowid.bytes + long_row.bytes +
+                     long_first.bytes + chunk_long.bytes + chunk_sum.bytes + chunk_count.bytes + xbuf.bytes);
+  }
+};
+
+bool up(DeviceBuffer& b, const void* src, size_t bytes, size_t extra = 64) {
+  if (!b.alloc(bytes + extra)) return false;
+  return bytes == 0 || VNEC_CUDA(cudaMemcpy(b.ptr, src, bytes, cudaMemcpyHostToDevice));
+}
+
+bool upload_batch(const BatchHost* h, int k, int precision, int wpb, BatchDev* d) {
+  const BatchHostView v = batch_view(h);
+  const size_t ne = (size_t)v.entries + 64;
+  if (!up(d->tasks, v.tasks, sizeof(SlicedTask) * (size_t)v.num_tasks) ||
+      !up(d->col, v.col, sizeof(int32_t) * ne, 0) || !up(d->rowid, v.rowid, 4 * (size_t)v.n_rowid) ||
+      !up(d->long_row, v.long_row, 4 * (size_t)v.num_long) ||
+      !up(d->long_first, v.long_first, 4 * (size_t)(v.num_long + 1)) ||
+      !up(d->chunk_long, v.chunk_long, 4 * (size_t)v.num_chunks) ||
+      !d->chunk_sum.alloc(sizeof(double) * ((size_t)v.num_chunks * k + 64)) ||
+      !d->chunk_count.alloc(sizeof(int) * ((size_t)v.num_long + 16)) ||
+      !VNEC_CUDA(cudaMemset(d->chunk_count.ptr, 0, d->chunk_count.bytes)))
+    return false;
+  if (precision == kPrecFP32) {
+    std::vector<float> f(ne);
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < (int64_t)ne; ++i) f[(size_t)i] = static_cast<float>(v.val[i]);
+    if (!up(d->val32, f.data(), sizeof(float) * ne, 0) ||
+        !d->xbuf.alloc(sizeof(float) * std::max<size_t>((size_t)v.n_cols * k, 1)))
+      return false;
+  } else if (!up(d->val, v.val, sizeof(double) * ne, 0)) {
+    return false;
+  }
+  BatchMatrix& m = d->m;
+  m.n_rows = v.n_rows;
+  m.n_cols = v.n_cols;
+  m.nnz = v.nnz;
+  m.entries = v.entries;
+  m.k = k;
+  m.lanes = v.lanes;
+  m.num_tasks = v.num_tasks;
+  m.num_long = v.num_long;
+  m.num_chunks = v.num_chunks;
+  m.tasks = d->tasks.as<SlicedTask>();
+  m.val = d->val.as<double>();
+  m.val32 = d->val32.as<float>();
+  m.col = d->col.as<int32_t>();
+  m.rowid = d->rowid.as<int32_t>();
+  m.long_row = d->long_row.as<int32_t>();
+  m.long_first = d->long_first.as<int32_t>();
+  m.chunk_long = d->chunk_long.as<int32_t>();
+  m.chunk_sum = d->chunk_sum.as<double>();
+  m.chunk_count = d->chunk_count.as<int>();
+  m.xbuf = d->xbuf.as<float>();
+  m.precision = precision;
+  m.warps_per_block = wpb;
+  m.grid = batch_grid(precision, k / v.lanes, wpb);
+  if (m.grid <= 0) {
+    set_error("batch: no occupancy for the kernel");
+    return false;
+  }
+  return true;
+}
+
+// Host CSR arrays of the batch in the builder's form (int64 offsets, int32 columns).
+struct BatchSource {
+  std::vector<int64_t> n_rows, n_cols;
+  std::vector<const int64_t*> rp;
+  std::vector<const int32_t*> ci;
+  std::vector<const double*> val;
+  std::vector<std::vector<int64_t>> own_rp;  // converted from 64-bit reference arrays
+  std::vector<std::vector<int32_t>> own_ci;
+  int size() const { return (int)n_rows.size(); }
+};
+
+bool make_source(int n, const CsrView* mats, BatchSource* s) {
+  s->own_rp.resize((size_t)n);
+  s->own_ci.resize((size_t)n);
+  for (int m = 0; m < n; ++m) {
+    const CsrView& v = mats[m];
+    s->n_rows.push_back(v.n_rows);
+    s->n_cols.push_back(v.n_cols);
+    s->val.push_back(static_cast<const double*>(v.val));
+    if (v.ptr) {
+      s->rp.push_back(v.ptr);
+    } else {
+      auto& o = s->own_rp[(size_t)m];
+      o.resize((size_t)v.n_rows + 1);
+      for (int64_t r = 0; r <= v.n_rows; ++r) o[(size_t)r] = v.row_begin(r);
+      s->rp.push_back(o.data());
+    }
+    if (v.idx) {
+      s->ci.push_back(v.idx);
+    } else {
+      auto& o = s->own_ci[(size_t)m];
+      o.resize((size_t)v.nnz);
+      for (int64_t q = 0; q < v.nnz; ++q) o[(size_t)q] = (int32_t)v.col_at(q);
+      s->ci.push_back(o.data());
+    }
+  }
+  return true;
+}
+
+BatchHost* build_host(const BatchSource& s, const std::vector<int>& pick, int k, const BatchParams& prm) {
+  std::vector<int64_t> nr, nc;
+  std::vector<const int64_t*> rp;
+  std::vector<const int32_t*> ci;
+  std::vector<const double*> val;
+  for (int m : pick) {
+    nr.push_back(s.n_rows[(size_t)m]);
+    nc.push_back(s.n_cols[(size_t)m]);
+    rp.push_back(s.rp[(size_t)m]);
+    ci.push_back(s.ci[(size_t)m]);
+    val.push_back(s.val[(size_t)m]);
+  }
+  return batch_build((int)pick.size(), nr.data(), nc.data(), rp.data(), ci.data(), val.data(), k, prm);
+}
+
+// ---------------------------------------------------------------------------
+// Autotuner.
+// ---------------------------------------------------------------------------
+
+struct TuneChoice {
+  int lanes = 0, long_len = 1024, wpb = 8;
+};
+
+std::mutex g_tune_mu;
+std::map<std::string, TuneChoice>& tune_cache() {
+  static auto* c = new std::map<std::string, TuneChoice>();
+  return *c;
+}
+
+int ilog2(int64_t v) {
+  int l = 0;
+  while (v > 1) {
+    v >>= 1;
+    ++l;
+  }
+  return l;
+}
+
+// Cache key: the device and driver, the call shape and coarse features of the
+// batch (log2 buckets of its size and row lengths).
+std::string tune_key(const BatchSource& s, int k, int precision) {
+  int dev = 0, drv = 0;
+  cudaGetDevice(&dev);
+  cudaDriverGetVersion(&drv);
+  cudaDeviceProp prop;
+  std::memset(&prop, 0, sizeof(prop));
+  cudaGetDeviceProperties(&prop, dev);
+  int64_t rows = 0, nnz = 0, maxlen = 0;
+  for (int m = 0; m < s.size(); ++m) {
+    rows += s.n_rows[(size_t)m];
+    nnz += s.rp[(size_t)m][s.n_rows[(size_t)m]];
+    for (int64_t r = 0; r < s.n_rows[(size_t)m]; ++r)
+      maxlen = std::max(maxlen, s.rp[(size_t)m][r + 1] - s.rp[(size_t)m][r]);
+  }
+  char buf[512];
+  std::snprintf(buf, sizeof(buf), "%s|sm%d|drv%d|k%d|p%d|n%d|r%d|z%d|a%d|m%d", prop.name, prop.multiProcessorCount,
+                drv, k, precision, ilog2(s.size()), ilog2(rows), ilog2(nnz), ilog2(rows ? 4 * nnz / rows : 0),
+                ilog2(maxlen));
+  for (char* c = buf; *c; ++c)
+    if (*c == '"' || *c == '\n') *c = '_';
+  return buf;
+}
+
+// Optional persistent cache: one JSON object per line in the file named by
+// VNEC_TUNE_CACHE, {"key": "...", "lanes": L, "long_row_len": N, "warps_per_block": W}.
+bool cache_file_lookup(const std::string& key, TuneChoice* c) {
+  const char* path = std::getenv("VNEC_TUNE_CACHE");
+  if (!path || !*path) return false;
+  FILE* f = std::fopen(path, "r");
+  if (!f) return false;
+  char line[1024];
+  bool found = false;
+  while (std::fgets(line, sizeof(line), f)) {
+    char k[600];
+    TuneChoice t;
+    if (std::sscanf(line, "{\"key\": \"%599[^\"]\", \"lanes\": %d, \"long_row_len\": %d, \"warps_per_block\": %d}", k,
+                    &t.lanes, &t.long_len, &t.wpb) == 4 &&
+        key == k) {
+      *c = t;
+      found = true;
+    }
+  }
+  std::fclose(f);
+  return found;
+}
+
+void cache_file_store(const std::string& key, const TuneChoice& c) {
+  const char* path = std::getenv("VNEC_TUNE_CACHE");
+  if (!path || !*path) return;
+  FILE* f = std::fopen(path, "a");
+  if (!f) return;
+  std::fprintf(f, "{\"key\": \"%s\", \"lanes\": %d, \"long_row_len\": %d, \"warps_per_block\": %d}\n", key.c_str(),
+               c.lanes, c.long_len, c.wpb);
+  std::fclose(f);
+}
+
+// Matrices timed by the tuner: evenly spaced in nnz order, enough of them to
+// hold `target` nonzeros (or the whole batch).
+std::vector<int> tune_sample(const BatchSource& s, int64_t target) {
+  const int n = s.size();
+  std::vector<int> order((size_t)n);
+  for (int m = 0; m < n; ++m) order[(size_t)m] = m;
+  auto nnz_of = [&](int m) { return s.rp[(size_t)m][s.n_rows[(size_t)m]]; };
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return nnz_of(a) < nnz_of(b); });
+  for (int cnt = std::min(n, 16);; cnt = std::min(n, cnt * 2)) {
+    std::vector<int> pick;
+    int64_t z = 0;
+    for (int i = 0; i < cnt; ++i) {
+      const int m = order[(size_t)((int64_t)i * n / cnt)];
+      pick.push_back(m);
+      z += nnz_of(m);
+    }
+    std::sort(pick.begin(), pick.end());
+    if (z >= target || cnt == n) return pick;
+  }
+}
+
+struct TuneRun {
+  std::vector<TuneChoice> cand;
+  std::vector<float> ms;
+  int best = -1;
+};
+
+float median_ms(std::vector<float> v) {
+  std::sort(v.begin(), v.end());
+  return v.empty() ? 0.f : v[v.size() / 2];
+}
+
+bool autotune(const BatchSource& s, int k, int precision, const SpB_VNEC_batch_options_ext* o, TuneRun* run) {
+  std::vector<int> lanes_c, long_c{256, 1024, 4096}, wpb_c{4, 8};
+  for (int L = 1; L <= 32; L <<= 1)
+    if (batch_supported(k, L)) lanes_c.push_back(L);
+  if (o->lanes > 0) lanes_c = {o->lanes};
+  if (o->long_row_len > 0) long_c = {o->long_row_len};
+  if (o->warps_per_block > 0) wpb_c = {o->warps_per_block};
+  const std::vector<int> pick = tune_sample(s, (int64_t)12 << 20);
+  cudaStream_t st = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  if (!VNEC_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking)) || !VNEC_CUDA(cudaEventCreate(&e0)) ||
+      !VNEC_CUDA(cudaEventCreate(&e1)))
+    return false;
+  DeviceBuffer X, Y;
+  bool ok = true;
+  for (int L : lanes_c) {
+    for (int ll : long_c) {
+      BatchParams prm;
+      prm.lanes = L;
+      prm.long_len = ll;
+      prm.chunk = o->chunk > 0 ? o->chunk : ll;
+      if (o->window_rows > 0) prm.window_rows = o->window_rows;
+      BatchHost* h = build_host(s, pick, k, prm);
+      if (!h) continue;
+      const BatchHostView hv = batch_view(h);
+      const size_t nx = (size_t)std::max<int64_t>(hv.n_cols, 1) * k, ny = (size_t)std::max<int64_t>(hv.n_rows, 1) * k;
+      if ((X.bytes < nx * 8 && !(X.release(), X.alloc(nx * 8))) || (Y.bytes < ny * 8 && !(Y.release(), Y.alloc(ny * 8))) ||
+          !VNEC_CUDA(cudaMemset(X.ptr, 0x3f, nx * 8))) {
+        batch_free(h);
+        ok = false;
+        break;
+      }
+      for (int wpb : wpb_c) {
+        BatchDev d;
+        if (!upload_batch(h, k, precision, wpb, &d)) {
+          ok = false;
+          break;
+        }
+        std::vector<float> t;
+        for (int rep = 0; rep < 7 && ok; ++rep) {
+          ok = VNEC_CUDA(cudaEventRecord(e0, st)) && batch_spmm(d.m, X.as<double>(), Y.as<double>(), st) &&
+               VNEC_CUDA(cudaEventRecord(e1, st)) && VNEC_CUDA(cudaEventSynchronize(e1));
+          float ms = 0.f;
+          if (ok && rep >= 2 && VNEC_CUDA(cudaEventElapsedTime(&ms, e0, e1))) t.push_back(ms);
+        }
+        if (!ok) break;
+        run->cand.push_back(TuneChoice{L, ll, wpb});
+        run->ms.push_back(median_ms(t));
+      }
+      batch_free(h);
+      if (!ok) break;
+    }
+    if (!ok) break;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaStreamDestroy(st);
+  if (!ok) return false;
+  for (size_t i = 0; i < run->ms.size(); ++i)
+    if (run->best < 0 || run->ms[i] < run->ms[(size_t)run->best]) run->best = (int)i;
+  if (run->best < 0) {
+    set_error("batch autotune: no candidate layout could be built");
+    return false;
+  }
+  return true;
+}
+
+// ---------------------------------------------------------------------------
+// Plan.
+// ---------------------------------------------------------------------------
+
+struct BatchPlan final : Plan {
+  BatchDev d;
+  BatchParams prm;
+  TuneRun tuning;
+  int precision = kPrecFP64;
+  bool use_graph = true;
+  std::vector<int64_t> row_off, col_off;
+  // Graph of the last (x, y) pair.
+  std::mutex gmu;
+  cudaStream_t cap = nullptr;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  const void* gx = nullptr;
+  void* gy = nullptr;
+
+  BatchPlan() : Plan(PlanKind::kBatch) {}
+  ~BatchPlan() override {
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+    if (cap) cudaStreamDestroy(cap);
+  }
+
+  bool capture(const void* d_x, void* d_y) {
+    if (!cap && !VNEC_CUDA(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking))) return false;
+    if (!VNEC_CUDA(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal))) return false;
+    const bool ok = batch_spmm(d.m, static_cast<const double*>(d_x), static_cast<double*>(d_y), cap);
+    cudaGraph_t g = nullptr;
+    const cudaError_t e = cudaStreamEndCapture(cap, &g);
+    if (!ok || !VNEC_CUDA(e)) {
+      if (g) cudaGraphDestroy(g);
+      return false;
+    }
+    if (exec) {
+      cudaGraphExecUpdateResultInfo info;
+      if (cudaGraphExecUpdate(exec, g, &info) != cudaSuccess) {
+        cudaGetLastError();
+        cudaGraphExecDestroy(exec);
+        exec = nullptr;
+      }
+    }
+    if (!exec && !VNEC_CUDA(cudaGraphInstantiate(&exec, g, 0))) {
+      cudaGraphDestroy(g);
+      return false;
+    }
+    if (graph) cudaGraphDestroy(graph);
+    graph = g;
+    gx = d_x;
+    gy = d_y;
+    return true;
+  }
+
+  bool run(const void* d_x, void* d_y, cudaStream_t s) override {
+    const int R = d.m.k / d.m.lanes;
+    if (R >= 2 && ((reinterpret_cast<uintptr_t>(d_x) | reinterpret_cast<uintptr_t>(d_y)) & 15)) {
+      set_error("batch: x and y must be 16-byte aligned for this plan's layout");
+      return false;
+    }
+    if (profiling) {
+      if (!ensure_events() || !VNEC_CUDA(cudaEventRecord(events[0], s))) return false;
+      if (!batch_spmm(d.m, static_cast<const double*>(d_x), static_cast<double*>(d_y), s)) return false;
+      return VNEC_CUDA(cudaEventRecord(events[1], s));
+    }
+    if (!use_graph) return batch_spmm(d.m, static_cast<const double*>(d_x), static_cast<double*>(d_y), s);
+    std::lock_guard<std::mutex> g(gmu);
+    if ((!exec || gx != d_x || gy != d_y) && !capture(d_x, d_y)) return false;
+    return VNEC_CUDA(cudaGraphLaunch(exec, s));
+  }
+  int kernel_ms(float* ms, int cap_n) const override {
+    if (!profiling || !events[0] || cap_n < 1) return 0;
+    if (cudaEventSynchronize(events[1]) != cudaSuccess) return 0;
+    cudaEventElapsedTime(&ms[0], events[0], events[1]);
+    return 1;
+  }
+  int launches_per_call() const override { return n_rows == 0 && precision != kPrecFP32 ? 0 : batch_launches(d.m); }
+  int64_t device_bytes() const override { return d.bytes() + (int64_t)(dx.bytes + dy.bytes); }
+  int64_t algorithmic_bytes() const override {
+    const int64_t vb = precision == kPrecFP32 ? 4 : 8;
+    return nnz * (vb + 4) + (n_rows + (int64_t)row_off.size() - 1) * 4 + (n_cols + n_rows) * rhs * 8;
+  }
+  void describe(SpB_VNEC_info_ext* info) const override {
+    info->kernel = SpB_VNEC_KERNEL_BATCH;
+    info->threads_per_block = d.m.warps_per_block * 32;
+    info->items_per_thread = d.m.k / d.m.lanes;
+    info->num_tiles = d.m.num_tasks;
+    info->blocks = d.m.grid;
+    info->precision = precision;
+    info->rhs = rhs;
+    info->lanes = d.m.lanes;
+    info->long_row_len = prm.long_len;
+  }
+};
+
+}  // namespace
+
+std::unique_ptr<Plan> build_batch(int n, const CsrView* mats, int k, const SpB_VNEC_batch_options_ext* opts) {
+  SpB_VNEC_batch_options_ext o;
+  std::memset(&o, 0, sizeof(o));
+  if (opts) o = *opts;
+  if (n < 1 || !mats) {
+    set_error("batch: no matrices");
+    return nullptr;
+  }
+  if (k < 1 || k > 32 || (k & (k - 1))) {
+    set_error("batch: k must be 1, 2, 4, 8, 16 or 32");
+    return nullptr;
+  }
+  if (o.precision != kPrecFP64 && o.precision != kPrecFP32) {
+    set_error("batch: precision must be SpB_VNEC_PREC_FP64 or SpB_VNEC_PREC_FP32");
+    return nullptr;
+  }
+  if (o.lanes > 0 && !batch_supported(k, o.lanes)) {
+    set_error("batch: lanes must divide 32 and k with k / lanes in {1, 2, 4, 8}");
+    return nullptr;
+  }
+  if (o.warps_per_block != 0 && o.warps_per_block != 4 && o.warps_per_block != 8) {
+    set_error("batch: warps_per_block must be 4 or 8");
+    return nullptr;
+  }
+  if (o.long_row_len < 0 || o.chunk < 0 || o.window_rows < 0) {
+    set_error("batch: negative option");
+    return nullptr;
+  }
+  auto p = std::make_unique<BatchPlan>();
+  p->type = SpB_FP64;
+  p->rhs = k;
+  p->precision = o.precision;
+  p->use_graph = o.no_graph == 0;
+  cudaGetDevice(&p->device);
+  p->row_off.assign((size_t)n + 1, 0);
+  p->col_off.assign((size_t)n + 1, 0);
+  for (int m = 0; m < n; ++m) {
+    const CsrView& v = mats[m];
+    if (v.type != SpB_FP64) {
+      set_error("batch: matrix " + std::to_string(m) + " is not FP64");
+      return nullptr;
+    }
+    if (!validate_csr(v, false)) {
+      set_error("batch: matrix " + std::to_string(m) + ": " + last_error());
+      return nullptr;
+    }
+    if (o.precision == kPrecFP32) {
+      const double* a = static_cast<const double*>(v.val);
+      for (int64_t q = 0; q < v.nnz; ++q)
+        if (!(std::fabs(a[q]) <= 3.4028234663852886e38)) {
+          set_error("batch FP32 form: a value of matrix " + std::to_string(m) + " is not finite in FP32");
+          return nullptr;
+        }
+    }
+    p->row_off[(size_t)m + 1] = p->row_off[(size_t)m] + v.n_rows;
+    p->col_off[(size_t)m + 1] = p->col_off[(size_t)m] + v.n_cols;
+    p->nnz += v.nnz;
+  }
+  p->n_rows = p->row_off[(size_t)n];
+  p->n_cols = p->col_off[(size_t)n];
+  BatchSource src;
+  make_source(n, mats, &src);
+
+  TuneChoice choice;
+  choice.lanes = o.lanes > 0 ? o.lanes : std::min(k, 32);
+  if (o.lanes == 0 && k >= 8) choice.lanes = k / 4;  // four right-hand sides per lane
+  if (o.long_row_len > 0) choice.long_len = o.long_row_len;
+  if (o.warps_per_block > 0) choice.wpb = o.warps_per_block;
+  if (o.autotune) {
+    const std::string key = tune_key(src, k, o.precision);
+    bool hit = false;
+    if (o.lanes == 0 && o.long_row_len == 0 && o.warps_per_block == 0) {
+      std::lock_guard<std::mutex> g(g_tune_mu);
+      auto it = tune_cache().find(key);
+      if (it != tune_cache().end()) {
+        choice = it->second;
+        hit = true;
+      } else if (cache_file_lookup(key, &choice)) {
+        tune_cache()[key] = choice;
+        hit = batch_supported(k, choice.lanes);
+      }
+    }
+    if (!hit) {
+      if (!autotune(src, k, o.precision, &o, &p->tuning)) return nullptr;
+      choice = p->tuning.cand[(size_t)p->tuning.best];
+      if (o.lanes == 0 && o.long_row_len == 0 && o.warps_per_block == 0) {
+        std::lock_guard<std::mutex> g(g_tune_mu);
+        tune_cache()[key] = choice;
+        cache_file_store(key, choice);
+      }
+    }
+  }
+  p->prm.lanes = choice.lanes;
+  p->prm.long_len = choice.long_len;
+  p->prm.chunk = o.chunk > 0 ? o.chunk : choice.long_len;
+  if (o.window_rows > 0) p->prm.window_rows = o.window_rows;
+  std::vector<int> all((size_t)n);
+  for (int m = 0; m < n; ++m) all[(size_t)m] = m;
+  BatchHost* h = build_host(src, all, k, p->prm);
+  if (!h) {
+    set_error("batch: more than 2^31 rows, columns or layout entries");
+    return nullptr;
+  }
+  const bool ok = upload_batch(h, k, o.precision, choice.wpb, &p->d);
+  batch_free(h);
+  if (!ok) return nullptr;
+  return p;
+}
+
+bool batch_offsets(const Plan* p, int64_t* row_off, int64_t* col_off) {
+  if (!p || p->kind != PlanKind::kBatch) return false;
+  const auto* b = static_cast<const BatchPlan*>(p);
+  if (row_off) std::copy(b->row_off.begin(), b->row_off.end(), row_off);
+  if (col_off) std::copy(b->col_off.begin(), b->col_off.end(), col_off);
+  return true;
+}
+
+int batch_size(const Plan* p) {
+  if (!p || p->kind != PlanKind::kBatch) return 0;
+  return (int)static_cast<const BatchPlan*>(p)->row_off.size() - 1;
+}
+
+int batch_tuning(const Plan* p, int* configs, float* ms, int cap, int* best) {
+  if (!p || p->kind != PlanKind::kBatch) return -1;
+  const TuneRun& t = static_cast<const BatchPlan*>(p)->tuning;
+  const int n = (int)t.cand.size();
+  for (int i = 0; i < n && i < cap; ++i) {
+    if (configs) {
+      configs[3 * i] = t.cand[(size_t)i].lanes;
+      configs[3 * i + 1] = t.cand[(size_t)i].long_len;
+      configs[3 * i + 2] = t.cand[(size_t)i].wpb;
+    }
+    if (ms) ms[i] = t.ms[(size_t)i];
+  }
+  if (best) *best = t.best;
+  return n;
+}
+
+}  // namespace vnec

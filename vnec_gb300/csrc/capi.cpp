@@ -3,6 +3,8 @@
 
 #include <cstdlib>
 #include <cstring>
+#include <string>
+#include <vector>
 #include <mutex>
 #include <type_traits>
 #include <unordered_map>
@@ -363,6 +365,54 @@ void* SpB_VNEC_plan_matrix_ext(const SpB_VNEC_options_ext* opts, const SpB_Matri
   return publish<VNEC_L>(std::move(p));
 }
 
+void* SpB_VNEC_batch_plan_ext(int n_mats, const int64_t* n_rows, const int64_t* n_cols, const int64_t* const* row_ptr,
+                              const int32_t* const* col, const double* const* val, int k,
+                              const SpB_VNEC_batch_options_ext* opts) {
+  clear_error();
+  if (n_mats < 1 || !n_rows || !n_cols || !row_ptr || !col || !val) {
+    set_error("SpB_VNEC_batch_plan_ext: invalid arguments");
+    return nullptr;
+  }
+  std::vector<CsrView> views((size_t)n_mats);
+  for (int m = 0; m < n_mats; ++m)
+    if (!view_from_arrays(SpB_FP64, n_rows[m], n_cols[m], row_ptr[m], col[m], val[m], &views[(size_t)m])) {
+      set_error("SpB_VNEC_batch_plan_ext: matrix " + std::to_string(m) + ": " + last_error());
+      return nullptr;
+    }
+  return publish<VNEC_L>(build_batch(n_mats, views.data(), k, opts));
+}
+
+void* SpB_VNEC_batch_plan_matrices_ext(int n_mats, const SpB_Matrix* A, int k, const SpB_VNEC_batch_options_ext* opts) {
+  clear_error();
+  if (n_mats < 1 || !A) {
+    set_error("SpB_VNEC_batch_plan_matrices_ext: invalid arguments");
+    return nullptr;
+  }
+  std::vector<CsrView> views((size_t)n_mats);
+  for (int m = 0; m < n_mats; ++m)
+    if (!view_from_matrix(A[m], &views[(size_t)m])) {
+      set_error("SpB_VNEC_batch_plan_matrices_ext: matrix " + std::to_string(m) + ": " + last_error());
+      return nullptr;
+    }
+  return publish<VNEC_L>(build_batch(n_mats, views.data(), k, opts));
+}
+
+SpB_Info SpB_VNEC_batch_offsets_ext(const void* plan, int64_t* row_offset, int64_t* col_offset) {
+  clear_error();
+  if (!batch_offsets(find_plan(plan), row_offset, col_offset)) {
+    set_error("SpB_VNEC_batch_offsets_ext: not a batch plan");
+    return SpB_FAILURE;
+  }
+  return SpB_SUCCESS;
+}
+
+int SpB_VNEC_batch_tuning_ext(const void* plan, int* configs, float* ms, int cap, int* best) {
+  clear_error();
+  const int n = batch_tuning(find_plan(plan), configs, ms, cap, best);
+  if (n < 0) set_error("SpB_VNEC_batch_tuning_ext: not a batch plan");
+  return n;
+}
+
 void SpB_VNEC_plan_free_ext(void* plan) {
   if (!plan) return;
   Plan* p = find_plan(plan);
@@ -428,6 +478,7 @@ SpB_Info SpB_VNEC_plan_info_ext(const void* plan, SpB_VNEC_info_ext* info) {
   std::memset(info, 0, sizeof(*info));
   p->describe(info);
   info->value_type = p->type;
+  info->rhs = p->rhs;
   info->n_rows = p->n_rows;
   info->n_cols = p->n_cols;
   info->nnz = p->nnz;

@@ -191,13 +191,12 @@ bool Plan::ensure_events() {
 bool Plan::run_host(const void* h_x, void* h_y) {
   const size_t vb = type == SpB_FP64 ? 8 : 4;
   if (!own_stream && !VNEC_CUDA(cudaStreamCreateWithFlags(&own_stream, cudaStreamNonBlocking))) return false;
-  if (!dx.ptr && !dx.alloc(vb * (size_t)std::max<int64_t>(n_cols, 1))) return false;
-  if (!dy.ptr && !dy.alloc(vb * (size_t)std::max<int64_t>(n_rows, 1))) return false;
-  if (n_cols > 0 && !VNEC_CUDA(cudaMemcpyAsync(dx.ptr, h_x, vb * n_cols, cudaMemcpyHostToDevice, own_stream)))
-    return false;
+  const size_t nx = (size_t)n_cols * rhs, ny = (size_t)n_rows * rhs;
+  if (!dx.ptr && !dx.alloc(vb * std::max<size_t>(nx, 1))) return false;
+  if (!dy.ptr && !dy.alloc(vb * std::max<size_t>(ny, 1))) return false;
+  if (nx > 0 && !VNEC_CUDA(cudaMemcpyAsync(dx.ptr, h_x, vb * nx, cudaMemcpyHostToDevice, own_stream))) return false;
   if (!run(dx.ptr, dy.ptr, own_stream)) return false;
-  if (n_rows > 0 && !VNEC_CUDA(cudaMemcpyAsync(h_y, dy.ptr, vb * n_rows, cudaMemcpyDeviceToHost, own_stream)))
-    return false;
+  if (ny > 0 && !VNEC_CUDA(cudaMemcpyAsync(h_y, dy.ptr, vb * ny, cudaMemcpyDeviceToHost, own_stream))) return false;
   return device_status(own_stream);
 }
 

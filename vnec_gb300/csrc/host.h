@@ -39,7 +39,7 @@ void convert_row_end(const CsrView& v, bool wide, void* out);
 void convert_cols(const CsrView& v, int32_t* out);
 
 // Kinds of plans this library builds.
-enum class PlanKind : int { kMergePath = 1, kWindowDense = 2, kWindowSliced = 3, kMixed = 4 };
+enum class PlanKind : int { kMergePath = 1, kWindowDense = 2, kWindowSliced = 3, kMixed = 4, kBatch = 5 };
 
 // Base of every plan.  The reference-typed public struct handed to callers is
 // a separate calloc'd block registered against the plan (see registry below).
@@ -47,6 +47,7 @@ struct Plan {
   PlanKind kind;
   SpB_Type type = SpB_FP64;  // value type of x and y
   int64_t n_rows = 0, n_cols = 0, nnz = 0;
+  int rhs = 1;  // right-hand sides: x is n_cols x rhs, y is n_rows x rhs (row-major)
   int device = 0;
   cudaStream_t own_stream = nullptr;
   DeviceBuffer dx, dy;  // staging for host-vector calls
@@ -82,6 +83,13 @@ std::unique_ptr<Plan> take_plan(const void* handle);
 std::unique_ptr<Plan> build_merge_path(const CsrView& v, const SpB_VNEC_options_ext* opts);
 std::unique_ptr<Plan> build_sliced(const CsrView& v, const SpB_VNEC_options_ext* opts);
 std::unique_ptr<Plan> build_dense(const CsrView& v, const SpB_VNEC_options_ext* opts);
+// Batched multi-right-hand-side plan over n CSR matrices (all FP64).
+std::unique_ptr<Plan> build_batch(int n, const CsrView* mats, int k, const SpB_VNEC_batch_options_ext* opts);
+// Row and column offsets of each matrix in a batch plan's concatenation (n + 1 each).
+bool batch_offsets(const Plan* p, int64_t* row_off, int64_t* col_off);
+int batch_size(const Plan* p);
+// Autotuner record of a batch plan (see SpB_VNEC_batch_tuning_ext); -1 if p is not a batch plan.
+int batch_tuning(const Plan* p, int* configs, float* ms, int cap, int* best);
 
 // Reference partition count and lane width constants used by IRD_VNEC.
 struct IrdParams {

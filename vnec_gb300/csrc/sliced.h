@@ -84,6 +84,8 @@ bool sliced_mixed_spmv(const SlicedMatrix& m, const SlicedMixed& mx, const doubl
                        cudaEvent_t* events = nullptr);
 // FP64 sliced kernel that only runs when *flag != 0 (DF32 fallback).
 bool sliced_guard_f64(const SlicedMatrix& m, const double* x, double* y, const int* flag, cudaStream_t s);
+// FP64 -> FP32 round-to-nearest-even of n values on stream s (one launch).
+bool round_to_f32(const double* x, float* x32, long long n, cudaStream_t s);
 inline int sliced_mixed_launches(const SlicedMatrix& m, int precision) {
   return 2 + (precision == kPrecDF32 ? 1 : 0) + (m.num_long > 0 || precision == kPrecDF32 ? 1 : 0);
 }

@@ -288,6 +288,14 @@ bool sliced_mixed_spmv(const SlicedMatrix& m, const SlicedMixed& mx, const doubl
   return true;
 }
 
+bool round_to_f32(const double* x, float* x32, long long n, cudaStream_t s) {
+  if (n <= 0) return true;
+  const int tb = 256;
+  const int grid = (int)std::min<long long>((n + tb - 1) / tb, 152LL * 16);
+  x_to_f32_kernel<<<grid, tb, 0, s>>>(x, x32, n);
+  return VNEC_CUDA(cudaGetLastError());
+}
+
 }  // namespace vnec
 
 extern "C" SpB_Info SpB_VNEC_f64_to_f32_ext(const double* d_in, float* d_out, int64_t n, void* stream) {

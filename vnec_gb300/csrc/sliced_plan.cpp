@@ -56,6 +56,7 @@ struct SlicedPlan final : Plan {
     info->num_tiles = m.num_tasks;
     info->blocks = blocks;
     info->precision = mx.precision;
+    info->long_row_len = prm.long_len;
   }
 };
 

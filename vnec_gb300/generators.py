@@ -148,3 +148,15 @@ def kat_values(m: HostCSR) -> tuple[HostCSR, np.ndarray]:
     rows = np.repeat(np.arange(m.n_rows, dtype=np.float64), np.diff(m.row_ptr))
     kat = HostCSR(m.n_rows, m.n_cols, m.row_ptr.copy(), m.col.copy(), rows)
     return kat, np.arange(m.n_cols, dtype=np.float64)
+
+
+def batch_lognormal(n_mats: int, *, rows_lo: int = 1000, rows_hi: int = 200_000, mu=float(np.log(8.0)),
+                    sigma=1.5, cap=4096, lo=-1.0, hi=1.0, seed=0) -> list[HostCSR]:
+    """Independent square CSR matrices with row counts log-uniform in
+    [rows_lo, rows_hi], lognormal row lengths (mu, sigma) capped at `cap`,
+    uniformly random distinct sorted columns and values U(lo, hi)."""
+    rng = np.random.default_rng(seed)
+    sizes = np.exp(rng.uniform(np.log(rows_lo), np.log(rows_hi), size=n_mats)).astype(np.int64)
+    sizes = np.maximum(sizes, 1)
+    return [lognormal(int(n), n_cols=int(n), mu=mu, sigma=sigma, cap=cap, lo=lo, hi=hi,
+                      seed=seed * 1_000_003 + i + 1) for i, n in enumerate(sizes)]
