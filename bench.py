@@ -333,13 +333,195 @@ def run_ours(args) -> None:
         torch.distributed.destroy_process_group()
 
 
+# ---------------------------------------------------------------------------
+# Batched multi-right-hand-side workload.
+# ---------------------------------------------------------------------------
+
+BATCH_DESC = ("512 square CSR matrices, rows log-uniform in [1e3, 2e5], row lengths lognormal(ln 8, 1.5) capped "
+              "at 4096, uniform distinct columns, values U(-1,1) FP64, seed 0; X row-major FP64 U(-1,1)")
+FP64_PEAK_TFLOPS = 1.25  # nominal GB300 FP64 (non-tensor) rate
+
+
+def batch_bytes(nnz: int, n_rows: int, n_cols: int, n_mats: int, k: int, vb: int = 8) -> int:
+    return nnz * (vb + 4) + (n_rows + n_mats) * 4 + (n_rows + n_cols) * k * 8
+
+
+def run_batch(args) -> None:
+    import torch
+
+    from vnec_gb300 import api
+    from vnec_gb300 import generators as G
+
+    ws, rank, local = dist_env()
+    if ws > 1:
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    else:
+        torch.cuda.set_device(0)
+    dev = torch.device("cuda", torch.cuda.current_device())
+    t_gen = time.time()
+    mats = G.batch_lognormal(args.batch_mats, seed=0)
+    t_gen = time.time() - t_gen
+    nnz = sum(m.nnz for m in mats)
+    n_rows = sum(m.n_rows for m in mats)
+    n_cols = sum(m.n_cols for m in mats)
+    ks = [int(v) for v in args.rhs.split(",")]
+    precs = [{"fp64": api.PREC_FP64, "fp32": api.PREC_FP32}[p] for p in args.batch_precision.split(",")]
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.int32, device=dev)
+    stream = torch.cuda.Stream(device=dev)
+    peak, peak_src = measured_peaks()
+    sampler = ClockSampler(dev.index)
+    w0 = time.time()
+    legs = {}
+    gpu_launches = 0
+    first = None
+    rng = np.random.default_rng(1)
+    for prec in precs:
+        for k in ks:
+            t_plan = time.time()
+            plan = api.BatchPlan(mats, k, precision=prec, autotune=True)
+            t_plan = time.time() - t_plan
+            info = plan.info()
+            ro, co = plan.offsets()
+            xv = rng.uniform(-1, 1, n_cols * k)
+            x = torch.from_numpy(xv).to(dev)
+            y = torch.empty(n_rows * k, dtype=torch.float64, device=dev)
+            B = batch_bytes(nnz, n_rows, n_cols, len(mats), k, 4 if prec == api.PREC_FP32 else 8)
+            with torch.cuda.stream(stream):
+                for _ in range(args.warmup):
+                    flush.fill_(1)
+                    plan.mxv_device(x.data_ptr(), y.data_ptr(), stream.cuda_stream)
+            stream.synchronize()
+            starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.batch_steps)]
+            ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.batch_steps)]
+            if ws > 1:
+                torch.distributed.barrier()
+            torch.cuda.synchronize()
+            with torch.cuda.stream(stream):
+                for i in range(args.batch_steps):
+                    flush.fill_(i)
+                    starts[i].record(stream)
+                    plan.mxv_device(x.data_ptr(), y.data_ptr(), stream.cuda_stream)
+                    ends[i].record(stream)
+            torch.cuda.synchronize()
+            ms = [a.elapsed_time(b) for a, b in zip(starts, ends)]
+            total = float(np.sum(ms))
+            if ws > 1:
+                t = torch.tensor([total], device=dev)
+                torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+                total = float(t.item())
+            gpu_launches += args.batch_steps * info.launches_per_call
+            value = B * args.batch_steps * ws / (total / 1e3) / 1e9
+            # end to end: pinned host X / Y through SpB_mxv_host_ext
+            hx = torch.from_numpy(xv).pin_memory()
+            hy = torch.empty(n_rows * k, dtype=torch.float64).pin_memory()
+            plan.mxv_host(hx.numpy(), hy.numpy())
+            e2e_steps = max(1, args.batch_steps // 4)
+            t0 = time.perf_counter()
+            for _ in range(e2e_steps):
+                plan.mxv_host(hx.numpy(), hy.numpy())
+            e2e_s = time.perf_counter() - t0
+            y_dev = y.cpu().numpy()
+            if not np.array_equal(hy.numpy(), y_dev):
+                raise RuntimeError("host-path and device-path batch results differ")
+            # accuracy on a sample of matrices against the compensated FP64 oracle
+            from oracle import oracle as O
+
+            errs = []
+            for i in range(0, len(mats), max(1, len(mats) // 16)):
+                m = mats[i]
+                Yr, cond = O.spmm_neumaier(m, xv[co[i] * k:co[i + 1] * k].reshape(m.n_cols, k))
+                Yg = y_dev[ro[i] * k:ro[i + 1] * k].reshape(m.n_rows, k)
+                errs.append(O.rowwise_error(Yg, Yr, cond).ravel())
+            rel = np.concatenate(errs)
+            cand, tms, best = plan.tuning()
+            mean_ms = total / args.batch_steps
+            leg = {"k": k, "precision": "fp32" if prec == api.PREC_FP32 else "fp64",
+                   "gbs": round(value, 2), "ms_per_step": round(mean_ms, 4),
+                   "hbm_frac": round(B / (mean_ms / 1e3) / 1e9 / peak, 4),
+                   "fp64_tflops": round(2 * nnz * k / (mean_ms / 1e3) / 1e12, 4),
+                   "e2e_gbs": round(B * e2e_steps / e2e_s / 1e9, 2),
+                   "h2d_bytes_per_step": n_cols * k * 8, "d2h_bytes_per_step": n_rows * k * 8,
+                   "algorithmic_bytes": B, "lanes": info.lanes, "long_row_len": info.long_row_len,
+                   "threads_per_block": info.threads_per_block, "tasks": info.num_tiles,
+                   "tuner": {"candidates": len(cand), "best_ms_on_sample": round(tms[best], 4) if cand else None,
+                             "worst_ms_on_sample": round(max(tms), 4) if cand else None},
+                   "plan_build_s": round(t_plan, 2), "launches_per_call": info.launches_per_call,
+                   "rel_error": {"max": float(rel.max()), "median": float(np.median(rel))}}
+            legs[f"{leg['precision']}_k{k}"] = leg
+            if first is None:
+                first = (leg, B)
+            plan.free()
+            del x, y, hx, hy
+            torch.cuda.empty_cache()
+    w1 = time.time()
+    clocks = sampler.stop(w0, w1)
+    leg, B = first
+    line = {
+        "metric": METRIC, "value": leg["gbs"], "unit": "GB/s", "n_gpus": ws, "steps": args.batch_steps,
+        "warmup": args.warmup, "ms_per_step": leg["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64" if leg["precision"] == "fp64" else "f32 (fp64 reductions)",
+        "data": "synthetic (seeded generator, resident in HBM before timing)",
+        "config": {"workload": "batch512_lognormal_" + leg["precision"] + f"_k{leg['k']}", "desc": BATCH_DESC,
+                   "n_mats": len(mats), "n_rows": n_rows, "n_cols": n_cols, "nnz": nnz, "k": leg["k"],
+                   "l2": "flushed before every timed step (512 MiB device write, outside the events)",
+                   "graph": "one CUDA graph replay per step (persistent kernel)", "gen_s": round(t_gen, 2)},
+        "roofline": {"bound": "hbm", "kernel": "batch_kernel", "achieved": round(B / (leg["ms_per_step"] / 1e3) / 1e9, 1),
+                     "peak": peak, "unit": "GB/s", "frac": leg["hbm_frac"], "peak_source": peak_src,
+                     "traffic": None, "fp64_tflops": leg["fp64_tflops"], "fp64_peak_tflops": FP64_PEAK_TFLOPS,
+                     "fp64_frac": round(leg["fp64_tflops"] / FP64_PEAK_TFLOPS, 4)},
+        "e2e": {"value": leg["e2e_gbs"], "unit": "GB/s", "h2d_bytes_per_step": leg["h2d_bytes_per_step"],
+                "d2h_bytes_per_step": leg["d2h_bytes_per_step"],
+                "path": "SpB_mxv_host_ext on a batch plan (pinned host X/Y)"},
+        "gpu_launches": gpu_launches, "clocks": clocks, "legs": legs,
+    }
+    if rank == 0 and ws == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = batch_cpu_baseline(mats, leg["k"], args.cpu_budget)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+
+
+def batch_cpu_baseline(mats, k: int, budget_s: float) -> dict:
+    """The reference's way to run a batch: SpMV_VNEC_L_FP64 per matrix and per
+    right-hand side (oracle port), timed on a sample of the matrices."""
+    from oracle import oracle as O
+
+    cores, nparts, arch = reference_cores_and_parts()
+    rng = np.random.default_rng(3)
+    order = np.argsort([m.nnz for m in mats])
+    pick = [mats[i] for i in order[::max(1, len(mats) // 32)]]
+    t_total, B_total, calls = 0.0, 0, 0
+    t_start = time.time()
+    for m in pick:
+        x = rng.uniform(-1, 1, m.n_cols)
+        t = O.time_L_f64(m, x, nparts, warm=1, reps=3)
+        t_total += t * k
+        B_total += batch_bytes(m.nnz, m.n_rows, m.n_cols, 1, k)
+        calls += 4
+        if time.time() - t_start > budget_s:
+            break
+    return {"value": round(B_total / t_total / 1e9, 3), "unit": "GB/s", "cores": cores, "kind": "port",
+            "sample": f"{len(pick)} of {len(mats)} matrices (every 16th in nnz order), SpMV_VNEC_L_FP64 restated "
+                      f"(oracle port) per matrix, 1 warm-up + 3 timed calls, x {k} right-hand sides; "
+                      f"{nparts} OpenMP threads on {cores} {arch} cores"}
+
+
 def main() -> None:
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", default="rmat24", choices=["rmat24", "rmat22", "uniform64k", "stencil256"])
+    ap.add_argument("--workload", default="rmat24",
+                    choices=["rmat24", "rmat22", "uniform64k", "stencil256", "batch512"])
+    ap.add_argument("--rhs", default="1,4,8,16,32", help="batch512: right-hand-side counts")
+    ap.add_argument("--batch-precision", default="fp64", help="batch512: fp64,fp32")
+    ap.add_argument("--batch-mats", type=int, default=512)
+    ap.add_argument("--batch-steps", type=int, default=10)
     ap.add_argument("--kernel", default="S", choices=["L", "S"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-budget", type=float, default=20.0, help="seconds of CPU-baseline timing")
@@ -348,6 +530,8 @@ def main() -> None:
         raise SystemExit("--warmup must be >= 3")
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "batch512":
+        run_batch(args)
     else:
         run_ours(args)
 
