@@ -129,7 +129,10 @@ typedef struct {
   int max_steps;         /* sliced: max 32-wide loads per lane for a row group (0: 32) */
   int cache_hints;       /* sliced: 0 default (streaming loads), 2 explicit L1/L2 evict policies */
   int precision;         /* sliced, FP64 matrices: SpB_VNEC_precision_ext */
-  int reserved[6];
+  int hot_columns;       /* sliced: hot-column window — the N most used columns get
+                            dense slots whose x values each call gathers once
+                            (0: library default, -1: off, N > 0: at most N) */
+  int reserved[5];
 } SpB_VNEC_options_ext;
 
 /* Precision forms of the sliced kernel for an FP64 matrix (x and y stay

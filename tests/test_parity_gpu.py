@@ -334,6 +334,50 @@ def test_sliced_edge_cases(built, name):
         p.free()
 
 
+HOT_SIZES = [1, 100, 4096, 1 << 20]
+
+
+@pytest.mark.parametrize("prec", [0, 1, 2, 3], ids=["fp64", "fp32", "bf16_rowscale", "df32_hilo"])
+def test_sliced_hot_column_window(built, prec):
+    """The hot-column window only relabels where x is read: every window size
+    gives the same bits as no window, for every precision form."""
+    from vnec_gb300 import api
+    from vnec_gb300 import generators as G
+
+    tol = PREC_TOL.get(prec, TOL_F64)
+    for m in (G.rmat(16, 16 << 16, seed=7), G.lognormal(20000, sigma=2.5, cap=4096, seed=8),
+              G.stencil27(20, seed=9), G.uniform_k(5000, 7, seed=2)):
+        xv = G.vector(m.n_cols, seed=9)
+        p0 = api.Plan(m, kernel=api.KERNEL_S, precision=prec, hot_columns=-1)
+        y0 = p0.mxv_host(xv)
+        p0.free()
+        check_f64(y0, m, xv, tol=tol)
+        for h in HOT_SIZES:
+            p = api.Plan(m, kernel=api.KERNEL_S, precision=prec, hot_columns=h, long_row_len=64)
+            y = p.mxv_host(xv)
+            check_f64(y, m, xv, tol=tol)
+            p.free()
+            p = api.Plan(m, kernel=api.KERNEL_S, precision=prec, hot_columns=h)
+            assert p.mxv_host(xv).tobytes() == y0.tobytes(), h
+            p.free()
+
+
+def test_sliced_hot_window_df32_guard(built):
+    """DF32 form with a hot window and an x outside the split range: the FP64
+    guard launch reads the hot slots through the window as well."""
+    from vnec_gb300 import api
+    from vnec_gb300 import generators as G
+
+    m = G.rmat(15, 16 << 15, seed=3)
+    p = api.Plan(m, kernel=api.KERNEL_S, precision=api.PREC_DF32, hot_columns=512)
+    xv = G.vector(m.n_cols, seed=4)
+    xv[::5] = 1e30
+    check_f64(p.mxv_host(xv), m, xv)
+    xg = G.vector(m.n_cols, seed=5)
+    check_f64(p.mxv_host(xg), m, xg)
+    p.free()
+
+
 def test_sliced_full_size_rmat_scale24(built):
     from vnec_gb300 import api
     from vnec_gb300 import generators as G

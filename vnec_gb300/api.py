@@ -62,7 +62,7 @@ class Options(C.Structure):
     _fields_ = [("kernel", C.c_int), ("threads_per_block", C.c_int), ("items_per_thread", C.c_int),
                 ("pipeline_stages", C.c_int), ("arithmetic", C.c_int), ("window_rows", C.c_int),
                 ("long_row_len", C.c_int), ("max_steps", C.c_int), ("cache_hints", C.c_int),
-                ("precision", C.c_int), ("reserved", C.c_int * 6)]
+                ("precision", C.c_int), ("hot_columns", C.c_int), ("reserved", C.c_int * 5)]
 
 
 class Info(C.Structure):
@@ -309,12 +309,12 @@ def SpB_mxv(y: Vector, A: Matrix, x: Vector, vnec: int | None = None) -> None:
 
 def options(kernel: int = KERNEL_AUTO, threads_per_block: int = 0, items_per_thread: int = 0,
             pipeline_stages: int = 0, arithmetic: int = ARITH_AUTO, window_rows: int = 0, long_row_len: int = 0,
-            max_steps: int = 0, cache_hints: int = 0, precision: int = PREC_FP64) -> Options:
+            max_steps: int = 0, cache_hints: int = 0, precision: int = PREC_FP64, hot_columns: int = 0) -> Options:
     o = Options()
     o.kernel, o.threads_per_block, o.items_per_thread = kernel, threads_per_block, items_per_thread
     o.pipeline_stages, o.arithmetic = pipeline_stages, arithmetic
     o.window_rows, o.long_row_len, o.max_steps = window_rows, long_row_len, max_steps
-    o.cache_hints, o.precision = cache_hints, precision
+    o.cache_hints, o.precision, o.hot_columns = cache_hints, precision, hot_columns
     return o
 
 

@@ -36,6 +36,13 @@ struct SlicedMatrix {
   void* chunk_sum = nullptr;            // num_chunks scratch (value type)
   int cache_hints = 0;                  // 0: streaming/read-only defaults, 1: explicit L1/L2 policies
   int vpe = 1;                          // values per entry: 1 (nonzeros) or 4 (dense blocks)
+  // Hot-column window: the `hot` most frequently used columns are relabelled
+  // n_cols + slot in `col`, and each call gathers their x values into a dense
+  // array (xhot for the FP64 kernel, the tail of the converted x for the
+  // precision forms), so the hottest part of x occupies consecutive sectors.
+  int hot = 0;
+  const int32_t* hot_cols = nullptr;  // original column of each slot
+  void* xhot = nullptr;               // FP64 kernel: hot x values
 };
 
 struct SlicedParams {
@@ -43,6 +50,7 @@ struct SlicedParams {
   int long_len = 1024;        // rows longer than this are split into chunks
   int chunk = 1024;           // entries per chunk (multiple of 32)
   int max_steps = 32;         // target load steps per lane for grouped rows
+  int hot = 0;                // hot-column window size (0: none)
 };
 
 // Host-side arrays of a built sliced matrix.
@@ -87,8 +95,9 @@ bool sliced_guard_f64(const SlicedMatrix& m, const double* x, double* y, const i
 // FP64 -> FP32 round-to-nearest-even of n values on stream s (one launch).
 bool round_to_f32(const double* x, float* x32, long long n, cudaStream_t s);
 inline int sliced_mixed_launches(const SlicedMatrix& m, int precision) {
-  return 2 + (precision == kPrecDF32 ? 1 : 0) + (m.num_long > 0 || precision == kPrecDF32 ? 1 : 0);
+  return 2 + (precision == kPrecDF32 ? 1 : 0) + (m.num_long > 0 || precision == kPrecDF32 ? 1 : 0) +
+         (precision == kPrecDF32 && m.hot > 0 ? 1 : 0);
 }
-inline int sliced_launches(const SlicedMatrix& m) { return m.num_long > 0 ? 2 : 1; }
+inline int sliced_launches(const SlicedMatrix& m) { return (m.num_long > 0 ? 2 : 1) + (m.hot > 0 ? 1 : 0); }
 
 }  // namespace vnec

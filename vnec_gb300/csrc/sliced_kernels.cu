@@ -13,6 +13,7 @@
 
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdint>
 
 #include "common.h"
@@ -139,11 +140,19 @@ dense_block_kernel(const SlicedTask* __restrict__ tasks, long long num_tasks, co
   }
 }
 
-template <typename V, int U, int H>
+// Address of x for a (possibly hot-relabelled) column.
+template <bool HOT, typename V>
+__device__ __forceinline__ const V* x_at(const V* __restrict__ x, const V* __restrict__ xh, int ncols, int c) {
+  if constexpr (HOT) return c < ncols ? x + c : xh + (c - ncols);
+  else return x + c;
+}
+
+template <typename V, int U, int H, bool HOT = false>
 __global__ void __launch_bounds__(kWarpsPerBlock * 32)
 sliced_kernel(const SlicedTask* __restrict__ tasks, long long num_tasks, const V* __restrict__ val,
               const int32_t* __restrict__ col, const int32_t* __restrict__ rowid, const V* __restrict__ x,
-              V* __restrict__ y, V* __restrict__ chunk_sum, const int* __restrict__ guard = nullptr) {
+              V* __restrict__ y, V* __restrict__ chunk_sum, const int* __restrict__ guard = nullptr,
+              const V* __restrict__ xh = nullptr, int ncols = 0) {
   if (guard && *reinterpret_cast<const volatile int*>(guard) == 0) return;
   const long long w = ((long long)blockIdx.x * kWarpsPerBlock) + (threadIdx.x >> 5);
   const int lane = threadIdx.x & 31;
@@ -169,12 +178,13 @@ sliced_kernel(const SlicedTask* __restrict__ tasks, long long num_tasks, const V
       v[u] = ld_stream_h<H>(vp + (k + u) * 32, pol);
     }
 #pragma unroll
-    for (int u = 0; u < U; ++u) xv[u] = ld_x_h<H>(x + c[u], pol);
+    for (int u = 0; u < U; ++u) xv[u] = ld_x_h<H>(x_at<HOT>(x, xh, ncols, c[u]), pol);
 #pragma unroll
     for (int u = 0; u < U; ++u) acc = fmav<V>(v[u], xv[u], acc);
   }
   for (; k < steps; ++k)
-    acc = fmav<V>(ld_stream_h<H>(vp + k * 32, pol), ld_x_h<H>(x + ld_stream_h<H>(cp + k * 32, pol), pol), acc);
+    acc = fmav<V>(ld_stream_h<H>(vp + k * 32, pol),
+                  ld_x_h<H>(x_at<HOT>(x, xh, ncols, ld_stream_h<H>(cp + k * 32, pol)), pol), acc);
   for (int off = (1 << vwl) >> 1; off > 0; off >>= 1) acc += __shfl_xor_sync(kFull, acc, off);
   if (kind == kSlicedChunk) {
     if (lane == 0) chunk_sum[row_base] = acc;
@@ -207,9 +217,15 @@ bool launch_dense(const SlicedMatrix& m, const void* x, void* y, cudaStream_t s)
   return VNEC_CUDA(cudaGetLastError());
 }
 
-template <typename V, int H>
+template <typename V>
+__global__ void gather_hot(const V* __restrict__ x, const int32_t* __restrict__ hot_cols, int n, V* __restrict__ xh) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) xh[i] = __ldg(x + __ldg(hot_cols + i));
+}
+
+template <typename V, int H, bool HOT>
 bool launch_main(const SlicedMatrix& m, const void* x, void* y, cudaStream_t s) {
-  auto kern = sliced_kernel<V, 8, H>;
+  auto kern = sliced_kernel<V, 8, H, HOT>;
   static bool configured = false;
   if (!configured) {
     // No shared memory: give the whole unified L1/shared array to L1.
@@ -221,9 +237,15 @@ bool launch_main(const SlicedMatrix& m, const void* x, void* y, cudaStream_t s) 
     set_error("sliced: too many tasks for one launch");
     return false;
   }
+  if (HOT) {
+    gather_hot<V><<<(unsigned)((m.hot + 255) / 256), 256, 0, s>>>(static_cast<const V*>(x), m.hot_cols, m.hot,
+                                                                  static_cast<V*>(m.xhot));
+    if (!VNEC_CUDA(cudaGetLastError())) return false;
+  }
   kern<<<(unsigned)grid, kWarpsPerBlock * 32, 0, s>>>(m.tasks, m.num_tasks, static_cast<const V*>(m.val), m.col,
                                                       m.rowid, static_cast<const V*>(x), static_cast<V*>(y),
-                                                      static_cast<V*>(m.chunk_sum), nullptr);
+                                                      static_cast<V*>(m.chunk_sum), nullptr,
+                                                      static_cast<const V*>(m.xhot), (int)m.n_cols);
   return VNEC_CUDA(cudaGetLastError());
 }
 
@@ -232,8 +254,9 @@ bool launch(const SlicedMatrix& m, const void* x, void* y, cudaStream_t s, cudaE
   if (ev && !VNEC_CUDA(cudaEventRecord(ev[0], s))) return false;
   if (m.num_tasks > 0) {
     const bool ok = m.vpe == 4       ? launch_dense<V>(m, x, y, s)
-                    : m.cache_hints ? launch_main<V, 1>(m, x, y, s)
-                                    : launch_main<V, 0>(m, x, y, s);
+                    : m.hot > 0     ? launch_main<V, 0, true>(m, x, y, s)
+                    : m.cache_hints ? launch_main<V, 1, false>(m, x, y, s)
+                                    : launch_main<V, 0, false>(m, x, y, s);
     if (!ok) return false;
   }
   if (ev && !VNEC_CUDA(cudaEventRecord(ev[1], s))) return false;
@@ -250,10 +273,21 @@ bool launch(const SlicedMatrix& m, const void* x, void* y, cudaStream_t s, cudaE
 }  // namespace
 
 bool sliced_guard_f64(const SlicedMatrix& m, const double* x, double* y, const int* flag, cudaStream_t s) {
+  // The guard only runs for DF32 plans, whose FP64 values sit in m.val and
+  // whose hot columns (if any) are served from x directly through hot_cols.
   const long long grid = (m.num_tasks + kWarpsPerBlock - 1) / kWarpsPerBlock;
-  sliced_kernel<double, 8, 0><<<(unsigned)grid, kWarpsPerBlock * 32, 0, s>>>(
-      m.tasks, m.num_tasks, static_cast<const double*>(m.val), m.col, m.rowid, x, y,
-      static_cast<double*>(m.chunk_sum), flag);
+  if (m.hot > 0) {
+    gather_hot<double><<<(unsigned)((m.hot + 255) / 256), 256, 0, s>>>(x, m.hot_cols, m.hot,
+                                                                       static_cast<double*>(m.xhot));
+    if (!VNEC_CUDA(cudaGetLastError())) return false;
+    sliced_kernel<double, 8, 0, true><<<(unsigned)grid, kWarpsPerBlock * 32, 0, s>>>(
+        m.tasks, m.num_tasks, static_cast<const double*>(m.val), m.col, m.rowid, x, y,
+        static_cast<double*>(m.chunk_sum), flag, static_cast<const double*>(m.xhot), (int)m.n_cols);
+  } else {
+    sliced_kernel<double, 8, 0><<<(unsigned)grid, kWarpsPerBlock * 32, 0, s>>>(
+        m.tasks, m.num_tasks, static_cast<const double*>(m.val), m.col, m.rowid, x, y,
+        static_cast<double*>(m.chunk_sum), flag);
+  }
   return VNEC_CUDA(cudaGetLastError());
 }
 

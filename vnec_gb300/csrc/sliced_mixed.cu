@@ -107,12 +107,27 @@ __global__ void x_to_f32_kernel(const double* __restrict__ x, float* __restrict_
 }
 namespace {
 
-__global__ void x_split_kernel(const double* __restrict__ x, float2* __restrict__ xs, long long n, int* flag) {
+// x (n values) followed by the values of the `nh` hot columns (a plan with a
+// hot-column window reads slot s as column n + s).
+__device__ __forceinline__ double x_ext(const double* __restrict__ x, long long n, const int32_t* __restrict__ hot,
+                                        long long i) {
+  return x[i < n ? i : __ldg(hot + (i - n))];
+}
+
+__global__ void x_to_f32_ext_kernel(const double* __restrict__ x, float* __restrict__ x32, long long n,
+                                    const int32_t* __restrict__ hot, int nh) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n + nh;
+       i += (long long)gridDim.x * blockDim.x)
+    x32[i] = f64_to_f32_rne(x_ext(x, n, hot, i));
+}
+
+__global__ void x_split_kernel(const double* __restrict__ x, float2* __restrict__ xs, long long n, int* flag,
+                               const int32_t* __restrict__ hot, int nh) {
   bool bad = false;
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n + nh;
        i += (long long)gridDim.x * blockDim.x) {
     float h, l;
-    bad |= !split_df(x[i], h, l);
+    bad |= !split_df(x_ext(x, n, hot, i), h, l);
     xs[i] = make_float2(h, l);
   }
   if (__syncthreads_or(bad) && threadIdx.x == 0) atomicExch(flag, 1);
@@ -248,14 +263,14 @@ bool sliced_mixed_spmv(const SlicedMatrix& m, const SlicedMixed& mx, const doubl
   if (ev && !VNEC_CUDA(cudaEventRecord(ev[0], s))) return false;
   const int tb = 256;
   const long long nx = m.n_cols;
-  const int xg = (int)std::min<long long>((nx + tb - 1) / tb, 152LL * 16);
+  const int xg = (int)std::min<long long>((nx + m.hot + tb - 1) / tb, 152LL * 16);
   int* flag = nullptr;
   if (nx > 0) {
     if (mx.precision == kPrecDF32) {
-      x_split_kernel<<<xg, tb, 0, s>>>(x, static_cast<float2*>(mx.xbuf), nx, mx.flag);
+      x_split_kernel<<<xg, tb, 0, s>>>(x, static_cast<float2*>(mx.xbuf), nx, mx.flag, m.hot_cols, m.hot);
       flag = mx.flag;
     } else {
-      x_to_f32_kernel<<<xg, tb, 0, s>>>(x, static_cast<float*>(mx.xbuf), nx);
+      x_to_f32_ext_kernel<<<xg, tb, 0, s>>>(x, static_cast<float*>(mx.xbuf), nx, m.hot_cols, m.hot);
     }
     if (!VNEC_CUDA(cudaGetLastError())) return false;
   }
