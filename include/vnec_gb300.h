@@ -106,8 +106,22 @@ typedef enum {
   SpB_VNEC_KERNEL_L = 1, /* merge-path CSR */
   SpB_VNEC_KERNEL_D = 2, /* windowed dense blocks */
   SpB_VNEC_KERNEL_S = 3, /* windowed sliced rows */
-  SpB_VNEC_KERNEL_BATCH = 4 /* batched multi-right-hand-side plans (SpB_VNEC_batch_plan_ext) */
+  SpB_VNEC_KERNEL_BATCH = 4, /* batched multi-right-hand-side plans (SpB_VNEC_batch_plan_ext) */
+  SpB_VNEC_KERNEL_HYBRID = 5, /* rows split by dense-block fill: dense blocks (D) / sliced rows (S) */
+  SpB_VNEC_KERNEL_LEARNED = 6, /* configuration predicted by the built-in MLP from matrix features;
+                                  exhaustive search for matrices outside its training range */
+  SpB_VNEC_KERNEL_SEARCH = 7,  /* exhaustive autotune: every configuration built and timed */
+  SpB_VNEC_KERNEL_RULE = 8     /* the reference harness's rule: L for >= 3e6 rows, else IRD_VNEC's D or S */
 } SpB_VNEC_kernel_ext;
+
+/* How a tuned plan's configuration was chosen (SpB_VNEC_plan_choice_ext). */
+typedef enum {
+  SpB_VNEC_CHOSEN_DIRECT = 0,   /* built with an explicit kernel */
+  SpB_VNEC_CHOSEN_LEARNED = 1,  /* the MLP's prediction */
+  SpB_VNEC_CHOSEN_SEARCH = 2,   /* exhaustive autotune (requested) */
+  SpB_VNEC_CHOSEN_RULE = 3,     /* the reference's rule */
+  SpB_VNEC_CHOSEN_FALLBACK = 4  /* exhaustive autotune after the learned choice declined */
+} SpB_VNEC_chosen_ext;
 
 /* Arithmetic of the FP64 merge-path kernel. */
 typedef enum {
@@ -132,7 +146,9 @@ typedef struct {
   int hot_columns;       /* sliced: hot-column window — the N most used columns get
                             dense slots whose x values each call gathers once
                             (0: library default, -1: off, N > 0: at most N) */
-  int reserved[5];
+  int dense_fill_permille; /* hybrid: rows whose dense-block fill (nnz / (4 x blocks))
+                              is at least this / 1000 use dense blocks (0: 500) */
+  int reserved[4];
 } SpB_VNEC_options_ext;
 
 /* Precision forms of the sliced kernel for an FP64 matrix (x and y stay
@@ -222,6 +238,60 @@ SpB_Info SpB_mxv_csr_noalloc_ext(int64_t n_rows, int64_t n_cols, int64_t nnz, co
                                  void *stream);
 
 SpB_Info SpB_VNEC_plan_info_ext(const void *plan, SpB_VNEC_info_ext *info);
+
+/* ---- Kernel selection (no counterpart in the reference, which fixes the
+ * choice in its test harness, test_spmv_vnec.cpp:197-245) ----
+ *
+ * Configuration space: SpB_VNEC_tune_configs_ext lists, per index, the kernel
+ * (L or HYBRID), its chunk (L: items per thread of a 256-thread merge-path
+ * tile; HYBRID: long-row chunk length) and the dense-block fill threshold in
+ * permille (HYBRID; 1 = every row dense, 1001 = every row sliced).  Returns
+ * the number of configurations (writes at most `cap`). */
+int SpB_VNEC_tune_configs_ext(int *kernel, int *chunk, int *permille, int cap);
+
+/* The 16 matrix features the learned choice reads, computed on the GPU from
+ * host CSR arrays (int64 offsets, int32 columns). */
+SpB_Info SpB_VNEC_features_ext(int64_t n_rows, int64_t n_cols, const int64_t *row_ptr, const int32_t *col,
+                               float *features);
+
+/* Exhaustive autotune: builds and times (median of `reps` calls, L2 flushed
+ * before each) every configuration; ms[i] = FLT_MAX where one cannot be
+ * built.  Returns the fastest index, -1 on failure.  `base` supplies the
+ * other options (precision, ...), may be NULL. */
+int SpB_VNEC_autotune_ext(const SpB_VNEC_options_ext *base, SpB_Type type, int64_t n_rows, int64_t n_cols,
+                          const int64_t *row_ptr, const int32_t *col, const void *val, int reps, float *ms);
+
+/* Configuration index the reference's rule and the built-in model choose
+ * (the latter also writes the predicted relative costs, log2 units, and
+ * whether a feature lies outside its training range).  -1 on failure or,
+ * for the learned choice, when no model is built in. */
+int SpB_VNEC_rule_choice_ext(SpB_Type type, int64_t n_rows, int64_t n_cols, const int64_t *row_ptr,
+                             const int32_t *col, const void *val);
+int SpB_VNEC_learned_choice_ext(SpB_Type type, int64_t n_rows, int64_t n_cols, const int64_t *row_ptr,
+                                const int32_t *col, const void *val, float *predicted, int *out_of_range);
+
+/* Configuration index and SpB_VNEC_chosen_ext of a plan built with kernel
+ * LEARNED / SEARCH / RULE (-1 / DIRECT otherwise). */
+SpB_Info SpB_VNEC_plan_choice_ext(const void *plan, int *config, int *how);
+
+/* The selection MLP: FP32, 16 -> 64 -> 64 -> one output per configuration
+ * (predicted log2 of its time over the fastest's), ReLU, trained with Adam on
+ * masked squared error by the library's own CUDA kernels.  Parameters as one
+ * array of SpB_VNEC_mlp_num_params_ext() floats: W1[64x16] b1 W2[64x64] b2
+ * W3[Cx64] b3 (row-major, out x in). */
+void *SpB_VNEC_mlp_create_ext(uint64_t seed);
+void SpB_VNEC_mlp_free_ext(void *model);
+int SpB_VNEC_mlp_num_params_ext(void);
+SpB_Info SpB_VNEC_mlp_params_ext(void *model, float *params, int set); /* set = 0: read, 1: write */
+SpB_Info SpB_VNEC_mlp_predict_ext(void *model, const float *X, int n, float *out);
+/* Loss and gradient (no update) of one batch: X n x 16, targets T and mask M n x C. */
+SpB_Info SpB_VNEC_mlp_grad_ext(void *model, const float *X, const float *T, const float *M, int n, float *loss,
+                               float *grad);
+SpB_Info SpB_VNEC_mlp_train_ext(void *model, const float *X, const float *T, const float *M, int n, int epochs,
+                                int batch, float lr, float weight_decay, uint64_t seed, float *loss_curve);
+/* The built-in model: returns 1 and copies its parameters and feature range
+ * (min, max per feature) when the library carries one, else 0. */
+int SpB_VNEC_builtin_model_ext(float *params, float *feature_range);
 
 /* Batched multi-right-hand-side mxv (no counterpart in the reference, whose
  * SpB_mxv multiplies one matrix by one vector).

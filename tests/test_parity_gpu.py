@@ -452,6 +452,41 @@ def test_dense_edge_cases(built, name):
         p.free()
 
 
+@pytest.mark.parametrize("permille", [1, 300, 500, 750, 1000, 1001])
+def test_hybrid_dense_sparse_split(built, permille):
+    """Rows split by dense-block fill between the dense-block and sliced
+    formats: every split point gives oracle-exact rows (permille 1: all rows
+    with a block go dense; 1001: none does)."""
+    from vnec_gb300 import api
+    from vnec_gb300 import generators as G
+
+    for m in (G.blockdiag(3000, 8, seed=1), G.banded(4000, 9, seed=2), G.lognormal(6000, sigma=2.0, cap=2000,
+                                                                                  seed=3),
+              G.rmat(14, 8 << 14, seed=4)):
+        xv = G.vector(m.n_cols, seed=5)
+        for kw in (dict(), dict(long_row_len=32, window_rows=500)):
+            p = api.Plan(m, kernel=api.KERNEL_HYBRID, dense_fill_permille=permille, **kw)
+            inf = p.info()
+            assert inf.kernel == api.KERNEL_HYBRID
+            y = p.mxv_host(xv)
+            check_f64(y, m, xv)
+            assert p.mxv_host(xv).tobytes() == y.tobytes()
+            p.free()
+
+
+@pytest.mark.parametrize("name", ["empty_matrix", "all_rows_empty", "single_entry", "rectangular_wide",
+                                  "hub_rows_and_empties"])
+def test_hybrid_edge_cases(built, name):
+    from vnec_gb300 import api
+
+    m = _edge_matrix(name)
+    xv = np.random.default_rng(2).uniform(-1, 1, size=m.n_cols)
+    for permille in (1, 500, 1001):
+        p = api.Plan(m, kernel=api.KERNEL_HYBRID, dense_fill_permille=permille)
+        check_f64(p.mxv_host(xv), m, xv)
+        p.free()
+
+
 def test_dense_blocks_reach_the_last_columns(built):
     """Blocks starting in the last 3 columns read x only inside the matrix."""
     from vnec_gb300 import api

@@ -25,7 +25,9 @@ SpB_FP32, SpB_FP64 = 10, 11
 SpB_DENSE = 0
 SpB_CSC, SpB_CSR = 0, 1
 SpB_VNEC_D, SpB_VNEC_S = 0, 1
-KERNEL_AUTO, KERNEL_L, KERNEL_D, KERNEL_S, KERNEL_BATCH = 0, 1, 2, 3, 4
+KERNEL_AUTO, KERNEL_L, KERNEL_D, KERNEL_S, KERNEL_BATCH, KERNEL_HYBRID = 0, 1, 2, 3, 4, 5
+KERNEL_LEARNED, KERNEL_SEARCH, KERNEL_RULE = 6, 7, 8
+CHOSEN_DIRECT, CHOSEN_LEARNED, CHOSEN_SEARCH, CHOSEN_RULE, CHOSEN_FALLBACK = 0, 1, 2, 3, 4
 ARITH_AUTO, ARITH_FP64, ARITH_DF32 = 0, 1, 2
 PREC_FP64, PREC_FP32, PREC_BF16, PREC_DF32 = 0, 1, 2, 3
 
@@ -62,7 +64,8 @@ class Options(C.Structure):
     _fields_ = [("kernel", C.c_int), ("threads_per_block", C.c_int), ("items_per_thread", C.c_int),
                 ("pipeline_stages", C.c_int), ("arithmetic", C.c_int), ("window_rows", C.c_int),
                 ("long_row_len", C.c_int), ("max_steps", C.c_int), ("cache_hints", C.c_int),
-                ("precision", C.c_int), ("hot_columns", C.c_int), ("reserved", C.c_int * 5)]
+                ("precision", C.c_int), ("hot_columns", C.c_int), ("dense_fill_permille", C.c_int),
+                ("reserved", C.c_int * 4)]
 
 
 class Info(C.Structure):
@@ -140,6 +143,37 @@ def lib() -> C.CDLL:
     L.SpB_VNEC_batch_offsets_ext.restype = C.c_int
     L.SpB_VNEC_batch_tuning_ext.argtypes = [_vp, _vp, _vp, C.c_int, C.POINTER(C.c_int)]
     L.SpB_VNEC_batch_tuning_ext.restype = C.c_int
+    _f = C.POINTER(C.c_float)
+    L.SpB_VNEC_tune_configs_ext.argtypes = [_vp, _vp, _vp, C.c_int]
+    L.SpB_VNEC_tune_configs_ext.restype = C.c_int
+    L.SpB_VNEC_features_ext.argtypes = [C.c_int64, C.c_int64, _vp, _vp, _vp]
+    L.SpB_VNEC_features_ext.restype = C.c_int
+    L.SpB_VNEC_autotune_ext.argtypes = [C.POINTER(Options), C.c_int, C.c_int64, C.c_int64, _vp, _vp, _vp, C.c_int,
+                                        _vp]
+    L.SpB_VNEC_autotune_ext.restype = C.c_int
+    L.SpB_VNEC_rule_choice_ext.argtypes = [C.c_int, C.c_int64, C.c_int64, _vp, _vp, _vp]
+    L.SpB_VNEC_rule_choice_ext.restype = C.c_int
+    L.SpB_VNEC_learned_choice_ext.argtypes = [C.c_int, C.c_int64, C.c_int64, _vp, _vp, _vp, _vp, _vp]
+    L.SpB_VNEC_learned_choice_ext.restype = C.c_int
+    L.SpB_VNEC_plan_choice_ext.argtypes = [_vp, _vp, _vp]
+    L.SpB_VNEC_plan_choice_ext.restype = C.c_int
+    L.SpB_VNEC_mlp_create_ext.argtypes = [C.c_uint64]
+    L.SpB_VNEC_mlp_create_ext.restype = _vp
+    L.SpB_VNEC_mlp_free_ext.argtypes = [_vp]
+    L.SpB_VNEC_mlp_free_ext.restype = None
+    L.SpB_VNEC_mlp_num_params_ext.argtypes = []
+    L.SpB_VNEC_mlp_num_params_ext.restype = C.c_int
+    L.SpB_VNEC_mlp_params_ext.argtypes = [_vp, _vp, C.c_int]
+    L.SpB_VNEC_mlp_params_ext.restype = C.c_int
+    L.SpB_VNEC_mlp_predict_ext.argtypes = [_vp, _vp, C.c_int, _vp]
+    L.SpB_VNEC_mlp_predict_ext.restype = C.c_int
+    L.SpB_VNEC_mlp_grad_ext.argtypes = [_vp, _vp, _vp, _vp, C.c_int, _f, _vp]
+    L.SpB_VNEC_mlp_grad_ext.restype = C.c_int
+    L.SpB_VNEC_mlp_train_ext.argtypes = [_vp, _vp, _vp, _vp, C.c_int, C.c_int, C.c_int, C.c_float, C.c_float,
+                                         C.c_uint64, _vp]
+    L.SpB_VNEC_mlp_train_ext.restype = C.c_int
+    L.SpB_VNEC_builtin_model_ext.argtypes = [_vp, _vp]
+    L.SpB_VNEC_builtin_model_ext.restype = C.c_int
     L._vnec_typed = True
     return L
 
@@ -309,12 +343,14 @@ def SpB_mxv(y: Vector, A: Matrix, x: Vector, vnec: int | None = None) -> None:
 
 def options(kernel: int = KERNEL_AUTO, threads_per_block: int = 0, items_per_thread: int = 0,
             pipeline_stages: int = 0, arithmetic: int = ARITH_AUTO, window_rows: int = 0, long_row_len: int = 0,
-            max_steps: int = 0, cache_hints: int = 0, precision: int = PREC_FP64, hot_columns: int = 0) -> Options:
+            max_steps: int = 0, cache_hints: int = 0, precision: int = PREC_FP64, hot_columns: int = 0,
+            dense_fill_permille: int = 0) -> Options:
     o = Options()
     o.kernel, o.threads_per_block, o.items_per_thread = kernel, threads_per_block, items_per_thread
     o.pipeline_stages, o.arithmetic = pipeline_stages, arithmetic
     o.window_rows, o.long_row_len, o.max_steps = window_rows, long_row_len, max_steps
     o.cache_hints, o.precision, o.hot_columns = cache_hints, precision, hot_columns
+    o.dense_fill_permille = dense_fill_permille
     return o
 
 
@@ -449,3 +485,141 @@ class BatchPlan(Plan):
         _check(n >= 0, "batch_tuning")
         n = min(n, cap)
         return [(cfg[3 * i], cfg[3 * i + 1], cfg[3 * i + 2]) for i in range(n)], [ms[i] for i in range(n)], best.value
+
+
+# --- kernel selection ---------------------------------------------------------
+
+NUM_FEATURES = 16
+
+
+def tune_configs() -> list[tuple[int, int, int]]:
+    """(kernel, chunk, dense-fill permille) of every tuner configuration."""
+    n = lib().SpB_VNEC_tune_configs_ext(None, None, None, 0)
+    k, c, p = (C.c_int * n)(), (C.c_int * n)(), (C.c_int * n)()
+    lib().SpB_VNEC_tune_configs_ext(k, c, p, n)
+    return [(k[i], c[i], p[i]) for i in range(n)]
+
+
+def _csr_args(csr):
+    rp = np.ascontiguousarray(csr.row_ptr, dtype=np.int64)
+    ci = np.ascontiguousarray(csr.col, dtype=np.int32)
+    vv = np.ascontiguousarray(csr.val, dtype=np.float64)
+    return rp, ci, vv
+
+
+def features(csr) -> np.ndarray:
+    """The 16 selection features of a CSR matrix, computed on the GPU."""
+    rp, ci, _ = _csr_args(csr)
+    out = np.zeros(NUM_FEATURES, dtype=np.float32)
+    _check(lib().SpB_VNEC_features_ext(csr.n_rows, csr.n_cols, rp.ctypes.data, ci.ctypes.data, out.ctypes.data)
+           == SpB_SUCCESS, "SpB_VNEC_features_ext")
+    return out
+
+
+def autotune(csr, reps: int = 5, opts: Options | None = None) -> tuple[np.ndarray, int]:
+    """Exhaustive autotune: median ms of every configuration (inf where unavailable), best index."""
+    rp, ci, vv = _csr_args(csr)
+    n = len(tune_configs())
+    ms = np.zeros(n, dtype=np.float32)
+    o = opts or options()
+    best = lib().SpB_VNEC_autotune_ext(C.byref(o), SpB_FP64, csr.n_rows, csr.n_cols, rp.ctypes.data, ci.ctypes.data,
+                                       vv.ctypes.data, reps, ms.ctypes.data)
+    _check(best >= 0, "SpB_VNEC_autotune_ext")
+    ms = ms.astype(np.float64)
+    ms[ms >= np.finfo(np.float32).max] = np.inf
+    return ms, best
+
+
+def rule_choice(csr) -> int:
+    rp, ci, vv = _csr_args(csr)
+    c = lib().SpB_VNEC_rule_choice_ext(SpB_FP64, csr.n_rows, csr.n_cols, rp.ctypes.data, ci.ctypes.data,
+                                       vv.ctypes.data)
+    _check(c >= 0, "SpB_VNEC_rule_choice_ext")
+    return c
+
+
+def learned_choice(csr) -> tuple[int, np.ndarray, bool]:
+    """Built-in model's choice, its predicted relative costs and the out-of-range flag."""
+    rp, ci, vv = _csr_args(csr)
+    n = len(tune_configs())
+    pred = np.zeros(n, dtype=np.float32)
+    ood = C.c_int(0)
+    c = lib().SpB_VNEC_learned_choice_ext(SpB_FP64, csr.n_rows, csr.n_cols, rp.ctypes.data, ci.ctypes.data,
+                                          vv.ctypes.data, pred.ctypes.data, C.byref(ood))
+    _check(c >= 0, "SpB_VNEC_learned_choice_ext")
+    return c, pred, bool(ood.value)
+
+
+def plan_choice(plan: "Plan") -> tuple[int, int]:
+    cfg, how = C.c_int(-1), C.c_int(0)
+    _check(lib().SpB_VNEC_plan_choice_ext(plan.h, C.byref(cfg), C.byref(how)) == SpB_SUCCESS, "plan_choice")
+    return cfg.value, how.value
+
+
+def builtin_model() -> tuple[np.ndarray, np.ndarray] | None:
+    n = lib().SpB_VNEC_mlp_num_params_ext()
+    p = np.zeros(n, dtype=np.float32)
+    r = np.zeros(2 * NUM_FEATURES, dtype=np.float32)
+    if not lib().SpB_VNEC_builtin_model_ext(p.ctypes.data, r.ctypes.data):
+        return None
+    return p, r.reshape(NUM_FEATURES, 2)
+
+
+class Mlp:
+    """The selection MLP, trained and evaluated by the library's CUDA kernels."""
+
+    def __init__(self, seed: int = 0):
+        self.h = lib().SpB_VNEC_mlp_create_ext(seed)
+        _check(bool(self.h), "SpB_VNEC_mlp_create_ext")
+        self.n_params = lib().SpB_VNEC_mlp_num_params_ext()
+        self.n_out = len(tune_configs())
+
+    @property
+    def params(self) -> np.ndarray:
+        p = np.zeros(self.n_params, dtype=np.float32)
+        _check(lib().SpB_VNEC_mlp_params_ext(self.h, p.ctypes.data, 0) == SpB_SUCCESS, "mlp_params")
+        return p
+
+    @params.setter
+    def params(self, p: np.ndarray) -> None:
+        p = np.ascontiguousarray(p, dtype=np.float32)
+        assert p.size == self.n_params
+        _check(lib().SpB_VNEC_mlp_params_ext(self.h, p.ctypes.data, 1) == SpB_SUCCESS, "mlp_params")
+
+    def predict(self, X: np.ndarray) -> np.ndarray:
+        X = np.ascontiguousarray(X, dtype=np.float32)
+        out = np.zeros((X.shape[0], self.n_out), dtype=np.float32)
+        _check(lib().SpB_VNEC_mlp_predict_ext(self.h, X.ctypes.data, X.shape[0], out.ctypes.data) == SpB_SUCCESS,
+               "mlp_predict")
+        return out
+
+    def loss_grad(self, X, T, M) -> tuple[float, np.ndarray]:
+        X = np.ascontiguousarray(X, dtype=np.float32)
+        T = np.ascontiguousarray(T, dtype=np.float32)
+        M = np.ascontiguousarray(M, dtype=np.float32)
+        g = np.zeros(self.n_params, dtype=np.float32)
+        loss = C.c_float(0)
+        _check(lib().SpB_VNEC_mlp_grad_ext(self.h, X.ctypes.data, T.ctypes.data, M.ctypes.data, X.shape[0],
+                                           C.byref(loss), g.ctypes.data) == SpB_SUCCESS, "mlp_grad")
+        return loss.value, g
+
+    def train(self, X, T, M, epochs=300, batch=64, lr=2e-3, weight_decay=1e-4, seed=1) -> np.ndarray:
+        X = np.ascontiguousarray(X, dtype=np.float32)
+        T = np.ascontiguousarray(T, dtype=np.float32)
+        M = np.ascontiguousarray(M, dtype=np.float32)
+        curve = np.zeros(epochs, dtype=np.float32)
+        _check(lib().SpB_VNEC_mlp_train_ext(self.h, X.ctypes.data, T.ctypes.data, M.ctypes.data, X.shape[0], epochs,
+                                            batch, lr, weight_decay, seed, curve.ctypes.data) == SpB_SUCCESS,
+               "mlp_train")
+        return curve
+
+    def free(self) -> None:
+        if self.h:
+            lib().SpB_VNEC_mlp_free_ext(self.h)
+            self.h = None
+
+    def __del__(self):  # pragma: no cover
+        try:
+            self.free()
+        except Exception:
+            pass

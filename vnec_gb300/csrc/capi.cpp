@@ -146,6 +146,12 @@ std::unique_ptr<Plan> build_from_view(const CsrView& v, const SpB_VNEC_options_e
       return build_sliced(v, opts);
     case SpB_VNEC_KERNEL_D:
       return build_dense(v, opts);
+    case SpB_VNEC_KERNEL_HYBRID:
+      return build_hybrid(v, opts);
+    case SpB_VNEC_KERNEL_LEARNED:
+    case SpB_VNEC_KERNEL_SEARCH:
+    case SpB_VNEC_KERNEL_RULE:
+      return build_tuned(v, opts);
     default:
       set_error("requested kernel is not available");
       return nullptr;

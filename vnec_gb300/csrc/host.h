@@ -39,7 +39,7 @@ void convert_row_end(const CsrView& v, bool wide, void* out);
 void convert_cols(const CsrView& v, int32_t* out);
 
 // Kinds of plans this library builds.
-enum class PlanKind : int { kMergePath = 1, kWindowDense = 2, kWindowSliced = 3, kMixed = 4, kBatch = 5 };
+enum class PlanKind : int { kMergePath = 1, kWindowDense = 2, kWindowSliced = 3, kMixed = 4, kBatch = 5, kHybrid = 6 };
 
 // Base of every plan.  The reference-typed public struct handed to callers is
 // a separate calloc'd block registered against the plan (see registry below).
@@ -48,6 +48,8 @@ struct Plan {
   SpB_Type type = SpB_FP64;  // value type of x and y
   int64_t n_rows = 0, n_cols = 0, nnz = 0;
   int rhs = 1;  // right-hand sides: x is n_cols x rhs, y is n_rows x rhs (row-major)
+  int tune_config = -1;  // configuration index chosen by the tuner (tuner.h), -1 if built directly
+  int tune_how = 0;      // SpB_VNEC_chosen_ext
   int device = 0;
   cudaStream_t own_stream = nullptr;
   DeviceBuffer dx, dy;  // staging for host-vector calls
@@ -81,8 +83,13 @@ std::unique_ptr<Plan> take_plan(const void* handle);
 
 // Plan builders.
 std::unique_ptr<Plan> build_merge_path(const CsrView& v, const SpB_VNEC_options_ext* opts);
-std::unique_ptr<Plan> build_sliced(const CsrView& v, const SpB_VNEC_options_ext* opts);
-std::unique_ptr<Plan> build_dense(const CsrView& v, const SpB_VNEC_options_ext* opts);
+// `keep` (optional): only rows with keep[r] != 0 are computed (the others' y is left alone).
+std::unique_ptr<Plan> build_sliced(const CsrView& v, const SpB_VNEC_options_ext* opts, const uint8_t* keep = nullptr);
+std::unique_ptr<Plan> build_dense(const CsrView& v, const SpB_VNEC_options_ext* opts, const uint8_t* keep = nullptr);
+// Row-level dense/sparse split between the two (options: dense_fill_permille).
+std::unique_ptr<Plan> build_hybrid(const CsrView& v, const SpB_VNEC_options_ext* opts);
+// Plans of kernel LEARNED / SEARCH / RULE (tuner.cpp).
+std::unique_ptr<Plan> build_tuned(const CsrView& v, const SpB_VNEC_options_ext* opts);
 // Batched multi-right-hand-side plan over n CSR matrices (all FP64).
 std::unique_ptr<Plan> build_batch(int n, const CsrView* mats, int k, const SpB_VNEC_batch_options_ext* opts);
 // Row and column offsets of each matrix in a batch plan's concatenation (n + 1 each).

@@ -34,7 +34,8 @@ struct SlicedMatrix {
   const int32_t* long_row = nullptr;    // num_long rows
   const int32_t* long_first = nullptr;  // num_long + 1 chunk offsets
   void* chunk_sum = nullptr;            // num_chunks scratch (value type)
-  int cache_hints = 0;                  // 0: streaming/read-only defaults, 1: explicit L1/L2 policies
+  int cache_hints = 0;                  // load cache-hint variant (sliced_kernels.cu), 0 default
+  int unroll = 8;                       // load steps in flight per lane: 4, 8, 12 or 16
   int vpe = 1;                          // values per entry: 1 (nonzeros) or 4 (dense blocks)
   // Hot-column window: the `hot` most frequently used columns are relabelled
   // n_cols + slot in `col`, and each call gathers their x values into a dense
@@ -58,10 +59,12 @@ struct SlicedHost;
 // `vpe` values per entry: 1 for the sliced format (one nonzero per entry),
 // the block width for the dense-block format (entry = block start column +
 // that many consecutive zero-padded values).
+// `keep` (optional, n_rows flags): rows with keep[r] == 0 get no task at all
+// (another plan writes their y).
 SlicedHost* sliced_build(int64_t n_rows, int64_t n_cols, const int64_t* row_ptr_or_null,
                          const uint64_t* row_ptr64_or_null, const int32_t* col_or_null,
                          const uint64_t* col64_or_null, const void* val, int value_bytes, const SlicedParams& prm,
-                         int vpe = 1);
+                         int vpe = 1, const uint8_t* keep = nullptr);
 void sliced_free(SlicedHost* h);
 // Uploads a built matrix; device buffers are owned by the caller-provided allocator.
 struct SlicedHostView {

@@ -56,7 +56,8 @@ inline int meta(int kind, int vwl, int nrows) { return kind | (vwl << 4) | (nrow
 }  // namespace
 
 SlicedHost* sliced_build(int64_t n_rows, int64_t n_cols, const int64_t* rp, const uint64_t* rp64, const int32_t* ci,
-                         const uint64_t* ci64, const void* val, int vb, const SlicedParams& prm, int vpe) {
+                         const uint64_t* ci64, const void* val, int vb, const SlicedParams& prm, int vpe,
+                         const uint8_t* keep) {
   // Each entry carries `vpe` consecutive values (1 for single nonzeros, the
   // block width for dense blocks); `vb` is the size of one value.
   const int eb = vb * vpe;
@@ -73,6 +74,7 @@ SlicedHost* sliced_build(int64_t n_rows, int64_t n_cols, const int64_t* rp, cons
     const int64_t r0 = w * W, r1 = std::min(n_rows, r0 + W);
     std::vector<int32_t> zero, grouped, longr;
     for (int64_t r = r0; r < r1; ++r) {
+      if (keep && !keep[r]) continue;
       const int64_t len = begin(r + 1) - begin(r);
       if (len == 0)
         zero.push_back((int32_t)r);

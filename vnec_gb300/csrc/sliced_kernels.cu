@@ -63,11 +63,45 @@ __device__ __forceinline__ float ld_keep(const float* p, unsigned long long pol)
   return v;
 }
 
+// Streamed value/column loads with no L1 allocation and no L2 policy.
+__device__ __forceinline__ double ld_na(const double* p) {
+  double v;
+  asm("ld.global.nc.L1::no_allocate.f64 %0, [%1];" : "=d"(v) : "l"(p));
+  return v;
+}
+__device__ __forceinline__ float ld_na(const float* p) {
+  float v;
+  asm("ld.global.nc.L1::no_allocate.f32 %0, [%1];" : "=f"(v) : "l"(p));
+  return v;
+}
+__device__ __forceinline__ int ld_na(const int* p) {
+  int v;
+  asm("ld.global.nc.L1::no_allocate.s32 %0, [%1];" : "=r"(v) : "l"(p));
+  return v;
+}
+__device__ __forceinline__ double ld_l1_keep(const double* p) {
+  double v;
+  asm("ld.global.nc.L1::evict_last.f64 %0, [%1];" : "=d"(v) : "l"(p));
+  return v;
+}
+__device__ __forceinline__ float ld_l1_keep(const float* p) {
+  float v;
+  asm("ld.global.nc.L1::evict_last.f32 %0, [%1];" : "=f"(v) : "l"(p));
+  return v;
+}
+
+// Cache-hint variants H: 0 streaming (.cs) loads of values/columns and
+// read-only x gathers; 1 explicit L1/L2 policies; 2 values/columns without L1
+// allocation; 3 as 2 with x gathers marked L1 evict-last.
 template <int H, typename T> __device__ __forceinline__ T ld_stream_h(const T* p, const Policies& pol) {
-  if constexpr (H == 0) return __ldcs(p); else return ld_once(p, pol.once);
+  if constexpr (H == 0) return __ldcs(p);
+  else if constexpr (H == 1) return ld_once(p, pol.once);
+  else return ld_na(p);
 }
 template <int H, typename T> __device__ __forceinline__ T ld_x_h(const T* p, const Policies& pol) {
-  if constexpr (H == 0) return __ldg(p); else return ld_keep(p, pol.keep);
+  if constexpr (H == 0 || H == 2) return __ldg(p);
+  else if constexpr (H == 1) return ld_keep(p, pol.keep);
+  else return ld_l1_keep(p);
 }
 
 
@@ -166,7 +200,8 @@ sliced_kernel(const SlicedTask* __restrict__ tasks, long long num_tasks, const V
   }
   const V* vp = val + base + lane;
   const int32_t* cp = col + base + lane;
-  const Policies pol = make_policies();
+  Policies pol{0, 0};
+  if constexpr (H == 1) pol = make_policies();
   V acc = V(0);
   int k = 0;
   for (; k + U <= steps; k += U) {
@@ -223,9 +258,9 @@ __global__ void gather_hot(const V* __restrict__ x, const int32_t* __restrict__ 
   if (i < n) xh[i] = __ldg(x + __ldg(hot_cols + i));
 }
 
-template <typename V, int H, bool HOT>
+template <typename V, int U, int H, bool HOT>
 bool launch_main(const SlicedMatrix& m, const void* x, void* y, cudaStream_t s) {
-  auto kern = sliced_kernel<V, 8, H, HOT>;
+  auto kern = sliced_kernel<V, U, H, HOT>;
   static bool configured = false;
   if (!configured) {
     // No shared memory: give the whole unified L1/shared array to L1.
@@ -249,14 +284,36 @@ bool launch_main(const SlicedMatrix& m, const void* x, void* y, cudaStream_t s) 
   return VNEC_CUDA(cudaGetLastError());
 }
 
+template <typename V, int U, bool HOT>
+bool launch_hints(const SlicedMatrix& m, const void* x, void* y, cudaStream_t s) {
+  switch (m.cache_hints) {
+    case 1: return launch_main<V, U, 1, HOT>(m, x, y, s);
+    case 2: return launch_main<V, U, 2, HOT>(m, x, y, s);
+    case 3: return launch_main<V, U, 3, HOT>(m, x, y, s);
+    default: return launch_main<V, U, 0, HOT>(m, x, y, s);
+  }
+}
+
+template <typename V, bool HOT>
+bool launch_unroll(const SlicedMatrix& m, const void* x, void* y, cudaStream_t s) {
+  switch (m.unroll) {
+    case 4: return launch_hints<V, 4, HOT>(m, x, y, s);
+    case 12: return launch_hints<V, 12, HOT>(m, x, y, s);
+    case 16: return launch_hints<V, 16, HOT>(m, x, y, s);
+    default: return launch_hints<V, 8, HOT>(m, x, y, s);
+  }
+}
+
+template <typename V>
+bool launch_variant(const SlicedMatrix& m, const void* x, void* y, cudaStream_t s) {
+  return m.hot > 0 ? launch_unroll<V, true>(m, x, y, s) : launch_unroll<V, false>(m, x, y, s);
+}
+
 template <typename V>
 bool launch(const SlicedMatrix& m, const void* x, void* y, cudaStream_t s, cudaEvent_t* ev) {
   if (ev && !VNEC_CUDA(cudaEventRecord(ev[0], s))) return false;
   if (m.num_tasks > 0) {
-    const bool ok = m.vpe == 4       ? launch_dense<V>(m, x, y, s)
-                    : m.hot > 0     ? launch_main<V, 0, true>(m, x, y, s)
-                    : m.cache_hints ? launch_main<V, 1, false>(m, x, y, s)
-                                    : launch_main<V, 0, false>(m, x, y, s);
+    const bool ok = m.vpe == 4 ? launch_dense<V>(m, x, y, s) : launch_variant<V>(m, x, y, s);
     if (!ok) return false;
   }
   if (ev && !VNEC_CUDA(cudaEventRecord(ev[1], s))) return false;

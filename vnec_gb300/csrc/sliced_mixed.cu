@@ -250,9 +250,13 @@ bool launch_mixed(const SlicedMatrix& m, const SlicedMixed& mx, const void* xs, 
     set_error("sliced: too many tasks for one launch");
     return false;
   }
-  sliced_mixed_kernel<C, 8><<<(unsigned)grid, kWarps * 32, 0, s>>>(
-      m.tasks, m.num_tasks, static_cast<const typename C::Val*>(m.val), m.col, m.rowid, xs, y,
-      static_cast<double*>(m.chunk_sum), mx.row_scale, mx.chunk_scale, flag);
+  auto kern = m.unroll == 4    ? sliced_mixed_kernel<C, 4>
+              : m.unroll == 12 ? sliced_mixed_kernel<C, 12>
+              : m.unroll == 16 ? sliced_mixed_kernel<C, 16>
+                               : sliced_mixed_kernel<C, 8>;
+  kern<<<(unsigned)grid, kWarps * 32, 0, s>>>(m.tasks, m.num_tasks, static_cast<const typename C::Val*>(m.val), m.col,
+                                              m.rowid, xs, y, static_cast<double*>(m.chunk_sum), mx.row_scale,
+                                              mx.chunk_scale, flag);
   return VNEC_CUDA(cudaGetLastError());
 }
 

@@ -54,7 +54,7 @@ struct SlicedPlan final : Plan {
   void describe(SpB_VNEC_info_ext* info) const override {
     info->kernel = kind == PlanKind::kWindowDense ? SpB_VNEC_KERNEL_D : SpB_VNEC_KERNEL_S;
     info->threads_per_block = 256;
-    info->items_per_thread = prm.max_steps;
+    info->items_per_thread = m.unroll;
     info->num_tiles = m.num_tasks;
     info->blocks = blocks;
     info->precision = mx.precision;
@@ -215,13 +215,19 @@ std::unique_ptr<Plan> upload(std::unique_ptr<SlicedPlan> p, SlicedHost* h, int v
   m.long_row = p->long_row.as<int32_t>();
   m.long_first = p->long_first.as<int32_t>();
   m.chunk_sum = p->chunk_sum.ptr;
-  m.cache_hints = (opts && opts->cache_hints == 2) ? 1 : 0;
+  // Options: cache_hints 2 explicit L1/L2 policies, 3 no L1 allocation for the
+  // streamed arrays, 4 the same with L1 evict-last x gathers; items_per_thread
+  // selects the unroll (4, 8, 12, 16; default 12, the fastest of the four on
+  // R-MAT 2^24 and the 256^3 stencil in FP64).
+  m.cache_hints = (opts && opts->cache_hints >= 2 && opts->cache_hints <= 4) ? opts->cache_hints - 1 : 0;
+  const int ipt = opts ? opts->items_per_thread : 0;
+  m.unroll = (ipt == 4 || ipt == 8 || ipt == 12 || ipt == 16) ? ipt : 12;
   return p;
 }
 
 }  // namespace
 
-std::unique_ptr<Plan> build_sliced(const CsrView& v, const SpB_VNEC_options_ext* opts) {
+std::unique_ptr<Plan> build_sliced(const CsrView& v, const SpB_VNEC_options_ext* opts, const uint8_t* keep) {
   if (!validate_csr(v, false)) return nullptr;
   auto p = std::make_unique<SlicedPlan>(PlanKind::kWindowSliced);
   p->type = v.type;
@@ -295,7 +301,7 @@ std::unique_ptr<Plan> build_sliced(const CsrView& v, const SpB_VNEC_options_ext*
     cols64 = nullptr;
     p->prm.hot = (int)p->hot_host.size();
   }
-  SlicedHost* h = sliced_build(v.n_rows, v.n_cols, v.ptr, v.ptr64, cols, cols64, src_val, vb, p->prm);
+  SlicedHost* h = sliced_build(v.n_rows, v.n_cols, v.ptr, v.ptr64, cols, cols64, src_val, vb, p->prm, 1, keep);
   if (!h) {
     set_error("sliced format: more than 2^31 entries or row slots");
     return nullptr;
@@ -310,7 +316,7 @@ std::unique_ptr<Plan> build_sliced(const CsrView& v, const SpB_VNEC_options_ext*
 // (the reference's grouping rule, :370-384, applied to global instead of
 // partition-compressed columns) — and the blocks are laid out as entries of
 // the sliced warp-task format.
-std::unique_ptr<Plan> build_dense(const CsrView& v, const SpB_VNEC_options_ext* opts) {
+std::unique_ptr<Plan> build_dense(const CsrView& v, const SpB_VNEC_options_ext* opts, const uint8_t* keep) {
   if (!validate_csr(v, true)) return nullptr;
   constexpr int W = 4;
   auto p = std::make_unique<SlicedPlan>(PlanKind::kWindowDense);
@@ -354,12 +360,110 @@ std::unique_ptr<Plan> build_dense(const CsrView& v, const SpB_VNEC_options_ext* 
   }
   p->blocks = nblocks;
   SlicedHost* h = sliced_build(v.n_rows, v.n_cols, bptr.data(), nullptr, bcol.data(), nullptr, bval.data(), vb,
-                               p->prm, W);
+                               p->prm, W, keep);
   if (!h) {
     set_error("dense-block format: more than 2^31 blocks or row slots");
     return nullptr;
   }
   return upload(std::move(p), h, vb, opts);
+}
+
+namespace {
+
+// Row-level dense/sparse split: rows whose dense-block fill (nonzeros / (4 x
+// blocks), blocks formed by the dense-block grouping rule) reaches the
+// threshold run in the dense-block format, the others in the sliced format.
+// It generalises the reference's matrix-level choice between VNEC-D and
+// VNEC-S (IRD against a fixed threshold, ird_calc.c:2-122 and
+// SpB_mxv.h:17-32) to single rows; threshold 0 gives the pure dense-block
+// plan, a threshold above 1 the pure sliced plan.
+struct HybridPlan final : Plan {
+  std::unique_ptr<Plan> dense, sparse;
+  int fill_permille = 500;
+  int64_t dense_rows = 0;
+  HybridPlan() : Plan(PlanKind::kHybrid) {}
+  bool run(const void* d_x, void* d_y, cudaStream_t s) override {
+    for (Plan* q : {dense.get(), sparse.get()}) {
+      if (!q) continue;
+      q->profiling = profiling;
+      if (!q->run(d_x, d_y, s)) return false;
+    }
+    return true;
+  }
+  int kernel_ms(float* ms, int cap) const override {
+    if (!profiling || cap < 2) return 0;
+    ms[0] = ms[1] = 0.f;
+    for (const Plan* q : {dense.get(), sparse.get()}) {
+      float part[8] = {0.f};
+      if (!q) continue;
+      const int n = q->kernel_ms(part, 8);
+      for (int i = 0; i < n && i < 2; ++i) ms[i] += part[i];
+    }
+    return 2;
+  }
+  int launches_per_call() const override {
+    return (dense ? dense->launches_per_call() : 0) + (sparse ? sparse->launches_per_call() : 0);
+  }
+  int64_t device_bytes() const override {
+    return (dense ? dense->device_bytes() : 0) + (sparse ? sparse->device_bytes() : 0);
+  }
+  int64_t algorithmic_bytes() const override {
+    const int64_t vb = type == SpB_FP64 ? 8 : 4;
+    return nnz * (vb + 4) + (n_rows + 1) * 4 + n_cols * vb + n_rows * vb;
+  }
+  void describe(SpB_VNEC_info_ext* info) const override {
+    if (sparse) sparse->describe(info);
+    else if (dense) dense->describe(info);
+    info->kernel = SpB_VNEC_KERNEL_HYBRID;
+    info->blocks = dense_rows;
+  }
+};
+
+}  // namespace
+
+std::unique_ptr<Plan> build_hybrid(const CsrView& v, const SpB_VNEC_options_ext* opts) {
+  if (!validate_csr(v, true)) return nullptr;
+  constexpr int W = 4;
+  auto p = std::make_unique<HybridPlan>();
+  p->type = v.type;
+  p->n_rows = v.n_rows;
+  p->n_cols = v.n_cols;
+  p->nnz = v.nnz;
+  cudaGetDevice(&p->device);
+  p->fill_permille = (opts && opts->dense_fill_permille > 0) ? opts->dense_fill_permille : 500;
+  // Row r goes dense when len_r * 1000 >= permille * 4 * blocks_r.
+  std::vector<uint8_t> is_dense((size_t)std::max<int64_t>(v.n_rows, 1), 0);
+  int64_t nd = 0;
+#pragma omp parallel for schedule(static) reduction(+ : nd)
+  for (int64_t r = 0; r < v.n_rows; ++r) {
+    int64_t nb = 0, cs = 0;
+    for (int64_t q = v.row_begin(r); q < v.row_begin(r + 1); ++q) {
+      const int64_t c = v.col_at(q);
+      if (nb == 0 || c - cs >= W) {
+        ++nb;
+        cs = c;
+      }
+    }
+    const int64_t len = v.row_begin(r + 1) - v.row_begin(r);
+    if (nb > 0 && len * 1000 >= (int64_t)p->fill_permille * W * nb) {
+      is_dense[(size_t)r] = 1;
+      ++nd;
+    }
+  }
+  p->dense_rows = nd;
+  SpB_VNEC_options_ext o;
+  std::memset(&o, 0, sizeof(o));
+  if (opts) o = *opts;
+  if (nd > 0) {
+    p->dense = build_dense(v, &o, nd == v.n_rows ? nullptr : is_dense.data());
+    if (!p->dense) return nullptr;
+  }
+  if (nd < v.n_rows) {
+    for (auto& f : is_dense) f = !f;
+    p->sparse = build_sliced(v, &o, nd == 0 ? nullptr : is_dense.data());
+    if (!p->sparse) return nullptr;
+  }
+  return p;
 }
 
 }  // namespace vnec
