@@ -18,7 +18,14 @@ copy peak), `e2e` (the same metric through the C-ABI host entry point with
 pinned host x and y, copies inside the timed region), `cpu_baseline` (the
 oracle's restatement of the reference's VNEC-L FP64 on this host's cores,
 reference protocol 1 warm-up + up to 40 calls), `clocks` (nvidia-smi sampled
-during the timed region), `rel_error` (against the compensated FP64 oracle).
+during the timed region), `rel_error` (against the compensated FP64 oracle),
+`legs` (per matrix — the headline matrix and, for R-MAT 2^24, the 256^3
+27-point stencil — the plain FP64 sliced kernel, its FP32 / BF16+row-scale /
+FP32 hi+lo forms and the learned and rule-based kernel selections: median ms
+over --leg-steps flushed calls, speed-up over plain FP64, row-wise error).
+
+`--workload batch512` measures the batched multi-right-hand-side form instead
+(512 uneven matrices, k = 1..32, one graph-replayed persistent launch per step).
 
 Multi-GPU: the path does not partition across GPUs in this build, so N GPUs
 run N independent replicas of the workload (scaling "weak").
@@ -166,6 +173,63 @@ def cpu_time_L(m, x, warm: int, reps: int, budget_s: float) -> tuple[float, int,
     reps = int(max(1, min(reps, budget_s / max(t1, 1e-9))))
     secs = O.time_L_f64(m, x, nparts, warm=0, reps=reps)
     return secs, reps, f"VNEC-L FP64 restated (oracle port), {nparts} OpenMP partitions/threads on {cores} {arch} cores"
+
+
+def time_plan_device(plan, x, y, flush, stream, steps: int, warmup: int) -> list[float]:
+    """CUDA-event times (ms) of `steps` device-path calls, L2 flushed before each."""
+    import torch
+
+    with torch.cuda.stream(stream):
+        for _ in range(warmup):
+            plan.mxv_device(x.data_ptr(), y.data_ptr(), stream.cuda_stream)
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+        for i, (a, b) in enumerate(ev):
+            flush.fill_(i)
+            a.record(stream)
+            plan.mxv_device(x.data_ptr(), y.data_ptr(), stream.cuda_stream)
+            b.record(stream)
+    torch.cuda.synchronize()
+    return [a.elapsed_time(b) for a, b in ev]
+
+
+def form_legs(m, xv, B: int, flush, stream, steps: int, warmup: int) -> dict:
+    """Plain FP64 and the precision forms of the sliced kernel on one matrix, plus
+    the learned kernel selection: median ms, throughput in the plain form's
+    algorithmic bytes (so ratios are time ratios), speed-up over plain FP64 and
+    row-wise error against the compensated FP64 oracle."""
+    import torch
+
+    from oracle import oracle as O
+    from vnec_gb300 import api
+
+    y_ref, cond = O.spmv_neumaier(m, xv)
+    x = torch.from_numpy(xv).to(flush.device)
+    y = torch.empty(m.n_rows, dtype=torch.float64, device=flush.device)
+    legs = {}
+    forms = [("fp64", dict(kernel=api.KERNEL_S)), ("fp32", dict(kernel=api.KERNEL_S, precision=api.PREC_FP32)),
+             ("bf16_rowscale", dict(kernel=api.KERNEL_S, precision=api.PREC_BF16)),
+             ("df32_hilo", dict(kernel=api.KERNEL_S, precision=api.PREC_DF32)),
+             ("learned", dict(kernel=api.KERNEL_LEARNED)), ("rule", dict(kernel=api.KERNEL_RULE))]
+    base = None
+    for name, kw in forms:
+        t0 = time.time()
+        plan = api.Plan(m, **kw)
+        build_s = time.time() - t0
+        ms = float(np.median(time_plan_device(plan, x, y, flush, stream, steps, warmup)))
+        rel = O.rowwise_error(y.cpu().numpy(), y_ref, cond)
+        leg = {"ms": round(ms, 5), "gbs_plain_bytes": round(B / ms / 1e6, 1), "launches": plan.info().launches_per_call,
+               "max_rel_error": float(rel.max()), "median_rel_error": float(np.median(rel)),
+               "plan_build_s": round(build_s, 2)}
+        if name in ("learned", "rule"):
+            cfg, how = api.plan_choice(plan)
+            leg["config"] = api.tune_configs()[cfg]
+            leg["how"] = ["direct", "learned", "search", "rule", "fallback-search"][how]
+        if base is None:
+            base = ms
+        leg["speedup_vs_fp64"] = round(base / ms, 3)
+        legs[name] = leg
+        plan.free()
+    return legs
 
 
 def run_reference(args) -> None:
@@ -321,6 +385,13 @@ def run_ours(args) -> None:
         "rel_error": {"max_rowwise": float(rel.max()), "median_rowwise": float(np.median(rel)),
                       "criterion": "|y-yhat| <= 1e-12 * sum|a x| (compensated FP64 oracle)"},
     }
+    if not args.no_legs:
+        legs = {args.workload: form_legs(m, xv, B, flush, stream, args.leg_steps, args.warmup)}
+        if args.workload == "rmat24":
+            m2, x2, _ = workload("stencil256")
+            legs["stencil256"] = form_legs(m2, x2, algorithmic_bytes(m2), flush, stream, args.leg_steps, args.warmup)
+            m2.free()
+        line["legs"] = legs
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         secs, reps, sample = cpu_time_L(m, xv, warm=1, reps=40, budget_s=args.cpu_budget)
         cores, _, _ = reference_cores_and_parts()
@@ -513,7 +584,7 @@ def batch_cpu_baseline(mats, k: int, budget_s: float) -> dict:
 def main() -> None:
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--steps", type=int, default=1000)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", default="rmat24",
@@ -524,6 +595,8 @@ def main() -> None:
     ap.add_argument("--batch-steps", type=int, default=10)
     ap.add_argument("--kernel", default="S", choices=["L", "S"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-legs", action="store_true", help="skip the precision-form / tuner legs")
+    ap.add_argument("--leg-steps", type=int, default=100)
     ap.add_argument("--cpu-budget", type=float, default=20.0, help="seconds of CPU-baseline timing")
     args = ap.parse_args()
     if args.warmup < 3:

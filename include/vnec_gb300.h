@@ -111,7 +111,8 @@ typedef enum {
   SpB_VNEC_KERNEL_LEARNED = 6, /* configuration predicted by the built-in MLP from matrix features;
                                   exhaustive search for matrices outside its training range */
   SpB_VNEC_KERNEL_SEARCH = 7,  /* exhaustive autotune: every configuration built and timed */
-  SpB_VNEC_KERNEL_RULE = 8     /* the reference harness's rule: L for >= 3e6 rows, else IRD_VNEC's D or S */
+  SpB_VNEC_KERNEL_RULE = 8,    /* the reference harness's rule: L for >= 3e6 rows, else IRD_VNEC's D or S */
+  SpB_VNEC_KERNEL_PUSH = 9     /* push-side SpMSpV plan: A held as CSC (SpB_VNEC_spmspv_ext) */
 } SpB_VNEC_kernel_ext;
 
 /* How a tuned plan's configuration was chosen (SpB_VNEC_plan_choice_ext). */
@@ -148,7 +149,10 @@ typedef struct {
                             (0: library default, -1: off, N > 0: at most N) */
   int dense_fill_permille; /* hybrid: rows whose dense-block fill (nnz / (4 x blocks))
                               is at least this / 1000 use dense blocks (0: 500) */
-  int reserved[4];
+  int transpose;         /* 1: the plan computes y := A^T x (the reference's SpB_TRAN0
+                            descriptor, OpenSparseBLAS.h:62-72): x has n_rows entries,
+                            y n_cols; any kernel, built on A's transpose */
+  int reserved[3];
 } SpB_VNEC_options_ext;
 
 /* Precision forms of the sliced kernel for an FP64 matrix (x and y stay
@@ -239,6 +243,20 @@ SpB_Info SpB_mxv_csr_noalloc_ext(int64_t n_rows, int64_t n_cols, int64_t nnz, co
 
 SpB_Info SpB_VNEC_plan_info_ext(const void *plan, SpB_VNEC_info_ext *info);
 
+/* Push-side sparse x sparse-vector product (SpMSpV): y := A x for a sparse x
+ * of nnz_x (index, value) pairs, on a plan built with kernel
+ * SpB_VNEC_KERNEL_PUSH (A held as its CSC).  Replaces the reference's
+ * declared-only SpB_vxm (OpenSparseBLAS.h:1940) for the push side of
+ * push/pull traversal: only the columns x selects are read.  y (n_rows
+ * values of the plan's type) is overwritten; additions into one y entry run
+ * as atomics, so results agree with the FP64 oracle to rounding but are not
+ * bit-reproducible.  An index outside [0, n_cols) is skipped and reported by
+ * SpB_VNEC_device_status_ext (the host variant reports it directly).  On a
+ * push plan, SpB_mxv_device_ext / SpB_mxv_host_ext take a dense x. */
+SpB_Info SpB_VNEC_spmspv_ext(void *plan, int64_t nnz_x, const int32_t *d_idx, const void *d_val, void *d_y,
+                             void *stream);
+SpB_Info SpB_VNEC_spmspv_host_ext(void *plan, int64_t nnz_x, const int32_t *idx, const void *val, void *y);
+
 /* ---- Kernel selection (no counterpart in the reference, which fixes the
  * choice in its test harness, test_spmv_vnec.cpp:197-245) ----
  *
@@ -308,7 +326,10 @@ int SpB_VNEC_builtin_model_ext(float *params, float *feature_range);
  * batch plan must not overlap on the GPU (they share the plan's long-row
  * scratch). */
 typedef struct {
-  int precision;       /* SpB_VNEC_PREC_FP64 (0) or SpB_VNEC_PREC_FP32 */
+  int precision;       /* SpB_VNEC_PREC_FP64 (0), SpB_VNEC_PREC_FP32 (FP32 values and products) or
+                          SpB_VNEC_PREC_DF32 (values and X as FP32 hi+lo pairs, double-float products
+                          and sums on the FP32 pipe: FP64-level error; needs |a| in [2^-40, 2^41) or 0,
+                          a call whose X leaves that range computes in FP64) */
   int lanes;           /* lanes per row (divides 32 and k, k / lanes in {1,2,4,8}); 0: tuned or default */
   int long_row_len;    /* rows longer than this are cut into chunks; 0: tuned or 1024 */
   int chunk;           /* entries per chunk; 0: long_row_len */
@@ -316,7 +337,8 @@ typedef struct {
   int autotune;        /* 1: time candidate layouts on a sample of the batch and keep the fastest */
   int no_graph;        /* 1: launch the kernels directly on each call */
   int window_rows;     /* rows sorted by length within windows of this size (0: 65536) */
-  int reserved[8];
+  int max_steps;       /* a row group spreads over enough slots to take at most this many steps (0: 32) */
+  int reserved[7];
 } SpB_VNEC_batch_options_ext;
 
 /* Plan from host CSR arrays per matrix: int64 row offsets (n_rows[m] + 1),

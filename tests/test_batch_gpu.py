@@ -15,7 +15,7 @@ from conftest import Csr
 
 pytestmark = pytest.mark.gpu
 
-TOL = {0: 1e-12, 1: 1e-6}
+TOL = {0: 1e-12, 1: 1e-6, 3: 1e-12}
 KS = [1, 2, 4, 8, 16, 32]
 
 
@@ -87,14 +87,14 @@ def _x(plan, k, seed=1):
 
 
 @pytest.mark.parametrize("k", KS)
-@pytest.mark.parametrize("precision", [0, 1])
+@pytest.mark.parametrize("precision", [0, 1, 3], ids=["fp64", "fp32", "df32"])
 def test_batch_all_lanes(built, batch, k, precision):
     """Every supported lanes-per-row layout, with a small long-row limit so that
     chunked rows (and the in-kernel long-row completion) are exercised."""
     from vnec_gb300 import api
 
     for L in lanes_for(k):
-        p = api.BatchPlan(batch, k, lanes=L, long_row_len=64, precision=precision)
+        p = api.BatchPlan(batch, k, lanes=L, long_row_len=64, precision=precision, max_steps=4)
         try:
             ro, co = p.offsets()
             X = _x(p, k)
@@ -125,6 +125,33 @@ def test_batch_default_layout_and_graph_off(built, batch, k):
         finally:
             p.free()
     assert outs[0].tobytes() == outs[1].tobytes()
+
+
+@pytest.mark.parametrize("k", [1, 4, 32])
+def test_batch_df32_guard_for_out_of_range_x(built, batch, k):
+    """X values outside the double-float split range switch the same launch to
+    FP64; the next in-range X runs double-float again."""
+    from vnec_gb300 import api
+
+    p = api.BatchPlan(batch, k, precision=api.PREC_DF32, long_row_len=64)
+    try:
+        ro, co = p.offsets()
+        for bad in (1e30, 3e-20, 5e-324, None):
+            X = _x(p, k, seed=6)
+            if bad is not None:
+                X[::13] = bad
+            Yref, cond = oracle_batch(batch, X, k, co, ro)
+            check(p.mxv_host(X), Yref, cond, TOL[3])
+    finally:
+        p.free()
+
+
+def test_batch_df32_rejects_out_of_range_values(built, batch):
+    from vnec_gb300 import api
+
+    bad = Csr(2, 2, [0, 1, 2], [0, 1], [1e-30, 2.0])
+    with pytest.raises(api.VnecError, match="DF32"):
+        api.BatchPlan([batch[0], bad], 4, precision=api.PREC_DF32)
 
 
 def test_batch_graph_pointer_changes(built, batch):

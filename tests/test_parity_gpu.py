@@ -474,6 +474,73 @@ def test_hybrid_dense_sparse_split(built, permille):
             p.free()
 
 
+def _transpose(m):
+    """CSR of A^T (stable: each transposed row keeps increasing original rows)."""
+    rows = np.repeat(np.arange(m.n_rows), np.diff(m.row_ptr))
+    order = np.argsort(np.asarray(m.col), kind="stable")
+    rp = np.concatenate([[0], np.cumsum(np.bincount(np.asarray(m.col), minlength=m.n_cols))])
+    from conftest import Csr
+
+    return Csr(m.n_cols, m.n_rows, rp, rows[order], np.asarray(m.val)[order])
+
+
+@pytest.mark.parametrize("kernel", ["L", "S", "D", "HYBRID", "RULE"])
+def test_transpose_spmv(built, kernel):
+    """y = A^T x (the reference's SpB_TRAN0 semantics) for every kernel, on
+    square and rectangular matrices."""
+    from vnec_gb300 import api
+    from vnec_gb300 import generators as G
+
+    k = getattr(api, "KERNEL_" + kernel)
+    mats = [G.rmat(14, 8 << 14, seed=4), G.lognormal(6000, n_cols=900, sigma=2.0, cap=800, seed=3),
+            _edge_matrix("rectangular_wide"), _edge_matrix("hub_rows_and_empties")]
+    for m in mats:
+        xv = np.random.default_rng(7).uniform(-1, 1, size=m.n_rows)
+        p = api.Plan(m, kernel=k, transpose=True)
+        inf = p.info()
+        assert (inf.n_rows, inf.n_cols) == (m.n_cols, m.n_rows)
+        y = p.mxv_host(xv)
+        check_f64(y, _transpose(m), xv)
+        p.free()
+
+
+@pytest.mark.parametrize("fp64", [True, False])
+def test_spmspv_push(built, fp64):
+    """Sparse x (a frontier of 0.1 % .. 100 % of the columns, duplicates
+    excluded) against the oracle on the dense equivalent; dense x on the same
+    plan; an out-of-range index is reported, not faulted."""
+    from vnec_gb300 import api
+    from vnec_gb300 import generators as G
+
+    dt = np.float64 if fp64 else np.float32
+    tol = TOL_F64 if fp64 else TOL_F32
+    rng = np.random.default_rng(9)
+    for m in (G.rmat(15, 8 << 15, seed=2), G.lognormal(9000, n_cols=4000, sigma=2.0, cap=3000, seed=4),
+              _edge_matrix("hub_rows_and_empties")):
+        p = api.Plan(m, kernel=api.KERNEL_PUSH, dtype=dt)
+        assert p.info().kernel == api.KERNEL_PUSH
+        for frac in (0.001, 0.05, 1.0):
+            nx = max(1, int(frac * m.n_cols))
+            idx = np.sort(rng.choice(m.n_cols, size=min(nx, m.n_cols), replace=False)).astype(np.int32)
+            xv = rng.uniform(-1, 1, idx.size)
+            dense = np.zeros(m.n_cols)
+            dense[idx] = xv.astype(dt)
+            y = p.spmspv_host(idx, xv)
+            check_f64(y.astype(np.float64), m if fp64 else _as32(m), dense, tol=tol)
+        xd = rng.uniform(-1, 1, m.n_cols)
+        check_f64(p.mxv_host(xd).astype(np.float64), m if fp64 else _as32(m), xd.astype(dt).astype(np.float64),
+                  tol=tol)
+        with pytest.raises(api.VnecError, match="outside"):
+            p.spmspv_host(np.array([0, m.n_cols + 5], dtype=np.int32), np.ones(2))
+        p.free()
+
+
+def _as32(m):
+    from conftest import Csr
+
+    return Csr(m.n_rows, m.n_cols, m.row_ptr, m.col, np.asarray(m.val, dtype=np.float32).astype(np.float64))
+
+
 @pytest.mark.parametrize("name", ["empty_matrix", "all_rows_empty", "single_entry", "rectangular_wide",
                                   "hub_rows_and_empties"])
 def test_hybrid_edge_cases(built, name):

@@ -26,7 +26,7 @@ SpB_DENSE = 0
 SpB_CSC, SpB_CSR = 0, 1
 SpB_VNEC_D, SpB_VNEC_S = 0, 1
 KERNEL_AUTO, KERNEL_L, KERNEL_D, KERNEL_S, KERNEL_BATCH, KERNEL_HYBRID = 0, 1, 2, 3, 4, 5
-KERNEL_LEARNED, KERNEL_SEARCH, KERNEL_RULE = 6, 7, 8
+KERNEL_LEARNED, KERNEL_SEARCH, KERNEL_RULE, KERNEL_PUSH = 6, 7, 8, 9
 CHOSEN_DIRECT, CHOSEN_LEARNED, CHOSEN_SEARCH, CHOSEN_RULE, CHOSEN_FALLBACK = 0, 1, 2, 3, 4
 ARITH_AUTO, ARITH_FP64, ARITH_DF32 = 0, 1, 2
 PREC_FP64, PREC_FP32, PREC_BF16, PREC_DF32 = 0, 1, 2, 3
@@ -65,7 +65,7 @@ class Options(C.Structure):
                 ("pipeline_stages", C.c_int), ("arithmetic", C.c_int), ("window_rows", C.c_int),
                 ("long_row_len", C.c_int), ("max_steps", C.c_int), ("cache_hints", C.c_int),
                 ("precision", C.c_int), ("hot_columns", C.c_int), ("dense_fill_permille", C.c_int),
-                ("reserved", C.c_int * 4)]
+                ("transpose", C.c_int), ("reserved", C.c_int * 3)]
 
 
 class Info(C.Structure):
@@ -84,7 +84,7 @@ class BatchOptions(C.Structure):
 
     _fields_ = [("precision", C.c_int), ("lanes", C.c_int), ("long_row_len", C.c_int), ("chunk", C.c_int),
                 ("warps_per_block", C.c_int), ("autotune", C.c_int), ("no_graph", C.c_int),
-                ("window_rows", C.c_int), ("reserved", C.c_int * 8)]
+                ("window_rows", C.c_int), ("max_steps", C.c_int), ("reserved", C.c_int * 7)]
 
 
 _vp = C.c_void_p
@@ -135,6 +135,10 @@ def lib() -> C.CDLL:
     L.SpB_VNEC_device_status_ext.restype = C.c_int
     L.SpB_VNEC_f64_to_f32_ext.argtypes = [_vp, _vp, C.c_int64, _vp]
     L.SpB_VNEC_f64_to_f32_ext.restype = C.c_int
+    L.SpB_VNEC_spmspv_ext.argtypes = [_vp, C.c_int64, _vp, _vp, _vp, _vp]
+    L.SpB_VNEC_spmspv_ext.restype = C.c_int
+    L.SpB_VNEC_spmspv_host_ext.argtypes = [_vp, C.c_int64, _vp, _vp, _vp]
+    L.SpB_VNEC_spmspv_host_ext.restype = C.c_int
     L.SpB_VNEC_batch_plan_ext.argtypes = [C.c_int, _vp, _vp, _vp, _vp, _vp, C.c_int, C.POINTER(BatchOptions)]
     L.SpB_VNEC_batch_plan_ext.restype = _vp
     L.SpB_VNEC_batch_plan_matrices_ext.argtypes = [C.c_int, _vp, C.c_int, C.POINTER(BatchOptions)]
@@ -344,13 +348,14 @@ def SpB_mxv(y: Vector, A: Matrix, x: Vector, vnec: int | None = None) -> None:
 def options(kernel: int = KERNEL_AUTO, threads_per_block: int = 0, items_per_thread: int = 0,
             pipeline_stages: int = 0, arithmetic: int = ARITH_AUTO, window_rows: int = 0, long_row_len: int = 0,
             max_steps: int = 0, cache_hints: int = 0, precision: int = PREC_FP64, hot_columns: int = 0,
-            dense_fill_permille: int = 0) -> Options:
+            dense_fill_permille: int = 0, transpose: bool = False) -> Options:
     o = Options()
     o.kernel, o.threads_per_block, o.items_per_thread = kernel, threads_per_block, items_per_thread
     o.pipeline_stages, o.arithmetic = pipeline_stages, arithmetic
     o.window_rows, o.long_row_len, o.max_steps = window_rows, long_row_len, max_steps
     o.cache_hints, o.precision, o.hot_columns = cache_hints, precision, hot_columns
     o.dense_fill_permille = dense_fill_permille
+    o.transpose = int(transpose)
     return o
 
 
@@ -392,6 +397,20 @@ class Plan:
         _check(lib().SpB_mxv_host_ext(self.h, x.ctypes.data, y.ctypes.data) == SpB_SUCCESS, "SpB_mxv_host_ext")
         return y
 
+    def spmspv_host(self, idx: np.ndarray, val: np.ndarray, y: np.ndarray | None = None) -> np.ndarray:
+        """y = A x for sparse x (push plans): idx int32 positions, val values."""
+        idx = np.ascontiguousarray(idx, dtype=np.int32)
+        val = np.ascontiguousarray(val, dtype=self.dtype)
+        if y is None:
+            y = np.empty(self.info().n_rows, dtype=self.dtype)
+        _check(lib().SpB_VNEC_spmspv_host_ext(self.h, idx.size, idx.ctypes.data, val.ctypes.data, y.ctypes.data)
+               == SpB_SUCCESS, "SpB_VNEC_spmspv_host_ext")
+        return y
+
+    def spmspv_device(self, nnz_x: int, d_idx: int, d_val: int, d_y: int, stream: int = 0) -> None:
+        _check(lib().SpB_VNEC_spmspv_ext(self.h, nnz_x, d_idx, d_val, d_y, stream or None) == SpB_SUCCESS,
+               "SpB_VNEC_spmspv_ext")
+
     def device_status(self, stream: int = 0) -> None:
         """Raises VnecError if a bounded device wait of this plan timed out."""
         _check(lib().SpB_VNEC_device_status_ext(self.h, stream or None) == SpB_SUCCESS, "device_status")
@@ -418,8 +437,9 @@ class Plan:
 
 def batch_options(precision: int = PREC_FP64, lanes: int = 0, long_row_len: int = 0, chunk: int = 0,
                   warps_per_block: int = 0, autotune: bool = False, graph: bool = True,
-                  window_rows: int = 0) -> BatchOptions:
+                  window_rows: int = 0, max_steps: int = 0) -> BatchOptions:
     o = BatchOptions()
+    o.max_steps = max_steps
     o.precision, o.lanes, o.long_row_len, o.chunk = precision, lanes, long_row_len, chunk
     o.warps_per_block, o.autotune, o.no_graph, o.window_rows = warps_per_block, int(autotune), int(not graph), \
         window_rows

@@ -6,8 +6,10 @@
 // r = row_offset[m] + local row, global column c = col_offset[m] + local
 // column, so X and Y are the matrices' blocks concatenated.  Tasks follow the
 // sliced layout idea (rows sorted by length, interleaved groups): L lanes
-// share one row and each owns k/L consecutive right-hand sides, so a warp
-// holds G = 32/L rows; entry j of group row g sits at base + j*G + g.
+// share one (value, column) slot and each owns k/L consecutive right-hand
+// sides, so a warp holds S = 32/L slots per step; a row spreads over V slots (V = 1..S chosen
+// per group of rows so that a row takes at most max_steps steps) and entry j
+// of group row g sits at base + (j / V) * S + g * V + j % V.
 #pragma once
 
 #include <cstdint>
@@ -24,7 +26,7 @@ struct BatchMatrix {
   int lanes = 1;      // lanes per row L (k % L == 0, 32 % L == 0)
   int64_t num_tasks = 0, num_long = 0, num_chunks = 0;
   const SlicedTask* tasks = nullptr;
-  const double* val = nullptr;
+  const void* val = nullptr;       // entries: double (FP64), float (FP32) or float2 hi/lo (DF32)
   const int32_t* col = nullptr;    // global columns
   const int32_t* rowid = nullptr;  // global rows
   const int32_t* long_row = nullptr;
@@ -34,9 +36,9 @@ struct BatchMatrix {
   int* chunk_count = nullptr;           // num_long arrival counters, 0 between calls
   int grid = 0;                         // persistent CTAs
   int warps_per_block = 8;
-  int precision = 0;                    // kPrecFP64 or kPrecFP32 (SlicedPrecision)
-  const float* val32 = nullptr;         // FP32 form: stored values
-  float* xbuf = nullptr;                // FP32 form: n_cols * k rounded X
+  int precision = 0;                    // kPrecFP64, kPrecFP32 or kPrecDF32 (SlicedPrecision)
+  void* xbuf = nullptr;                 // FP32 / DF32: n_cols * k converted X
+  int* flag = nullptr;                  // DF32: X outside the split range this call
 };
 
 struct BatchParams {
@@ -44,6 +46,7 @@ struct BatchParams {
   int long_len = 1024;    // rows longer than this become chunks
   int chunk = 1024;       // entries per chunk
   int window_rows = 1 << 16;
+  int max_steps = 32;     // slots per row chosen so that a row takes at most this many steps
 };
 
 struct BatchHost;
@@ -72,6 +75,6 @@ int batch_grid(int precision, int rhs_per_lane, int warps_per_block);
 // rounds X into xbuf).  Long rows are finished inside the kernel by the last
 // of their chunks to arrive.
 bool batch_spmm(const BatchMatrix& m, const double* X, double* Y, cudaStream_t s);
-inline int batch_launches(const BatchMatrix& m) { return m.precision == kPrecFP32 ? 2 : 1; }
+inline int batch_launches(const BatchMatrix& m) { return m.precision == kPrecFP64 ? 1 : 2; }
 
 }  // namespace vnec

@@ -3,12 +3,13 @@
 // The batch of matrices is laid out as its block-diagonal concatenation.
 // Within windows of `window_rows` global rows, rows are split into empty rows
 // (ZERO tasks of up to 32 rows), grouped rows (len <= long_len) sorted by
-// length and packed G = 32 / lanes to a task, and long rows cut into chunks of
-// `chunk` entries.  Entry j of group slot g of a task sits at base + j*G + g,
-// so at every step the warp reads G consecutive (value, column) pairs; a chunk
-// keeps its entries contiguous (entry j is read at step j / G by slot j % G).
-// Padding entries carry value 0 and a column of their own row, whose x row the
-// lane has already read.
+// length, and long rows cut into chunks of `chunk` entries.  A warp reads
+// S = 32 / lanes (value, column) slots per step.  Grouped rows are packed
+// G = S / V to a task, V = 2^vwl slots per row, V the smallest power of two
+// (<= S) that keeps the group's longest row within max_steps steps; entry j
+// of row g sits at base + (j / V) * S + g * V + j % V.  A chunk uses all S
+// slots (entry j at base + j).  Padding entries carry value 0 and a column of
+// their own row, whose x row the lane has already read.
 
 #include <omp.h>
 
@@ -32,7 +33,14 @@ struct BatchHost {
 
 namespace {
 
-inline int meta(int kind, int nrows) { return kind | (nrows << 8); }
+inline int meta(int kind, int vwl, int nrows) { return kind | (vwl << 4) | (nrows << 8); }
+
+// Smallest vwl (V = 2^vwl <= 2^max_vwl) with ceil(len / V) <= max_steps.
+inline int vwl_for(int64_t len, int max_steps, int max_vwl) {
+  int l = 0;
+  while (l < max_vwl && ((len + (1 << l) - 1) >> l) > max_steps) ++l;
+  return l;
+}
 
 struct Window {
   std::vector<SlicedTask> tasks;  // base / row_base relative to the window
@@ -60,8 +68,11 @@ struct Source {
 BatchHost* batch_build(int n, const int64_t* n_rows, const int64_t* n_cols, const int64_t* const* row_ptr,
                        const int32_t* const* col, const double* const* val, int k, const BatchParams& prm) {
   const int L = prm.lanes > 0 ? prm.lanes : std::min(k, 32);
-  if (!batch_supported(k, L) || prm.long_len < 1 || prm.chunk < 1 || prm.window_rows < 1) return nullptr;
-  const int G = 32 / L;
+  if (!batch_supported(k, L) || prm.long_len < 1 || prm.chunk < 1 || prm.window_rows < 1 || prm.max_steps < 1)
+    return nullptr;
+  const int S = 32 / L;  // slots per step
+  int max_vwl = 0;
+  while ((2 << max_vwl) <= S) ++max_vwl;
   std::vector<int64_t> row_off((size_t)n + 1, 0), col_off((size_t)n, 0);
   int64_t nc = 0, nnz = 0;
   for (int m = 0; m < n; ++m) {
@@ -103,16 +114,25 @@ BatchHost* batch_build(int n, const int64_t* n_rows, const int64_t* n_cols, cons
     std::stable_sort(grouped.begin(), grouped.end(), [&](int32_t a, int32_t b) { return L_of(a) < L_of(b); });
     for (size_t i = 0; i < zero.size(); i += 32) {
       const int c = (int)std::min<size_t>(32, zero.size() - i);
-      wd.tasks.push_back(SlicedTask{0, (int32_t)wd.rowid.size(), 0, meta(kSlicedZero, c)});
+      wd.tasks.push_back(SlicedTask{0, (int32_t)wd.rowid.size(), 0, meta(kSlicedZero, 0, c)});
       for (int q = 0; q < c; ++q) wd.rowid.push_back(zero[i + q]);
     }
-    for (size_t i = 0; i < grouped.size(); i += (size_t)G) {
-      const int c = (int)std::min<size_t>((size_t)G, grouped.size() - i);
-      const int64_t steps = L_of(grouped[i + c - 1]);
-      wd.tasks.push_back(
-          SlicedTask{(int32_t)wd.entries, (int32_t)wd.rowid.size(), (int32_t)steps, meta(kSlicedRows, c)});
-      for (int q = 0; q < c; ++q) wd.rowid.push_back(grouped[i + q]);
-      wd.entries += steps * G;
+    size_t i = 0;
+    while (i < grouped.size()) {
+      int vwl = vwl_for(L_of(grouped[i]), prm.max_steps, max_vwl);
+      size_t c = std::min<size_t>((size_t)(S >> vwl), grouped.size() - i);
+      // The group's longest row may need a wider V (fewer rows per group).
+      while (vwl_for(L_of(grouped[i + c - 1]), prm.max_steps, max_vwl) > vwl) {
+        ++vwl;
+        c = std::min<size_t>((size_t)(S >> vwl), grouped.size() - i);
+      }
+      const int64_t V = (int64_t)1 << vwl;
+      const int64_t steps = (L_of(grouped[i + c - 1]) + V - 1) / V;
+      wd.tasks.push_back(SlicedTask{(int32_t)wd.entries, (int32_t)wd.rowid.size(), (int32_t)steps,
+                                    meta(kSlicedRows, vwl, (int)c)});
+      for (size_t q = 0; q < c; ++q) wd.rowid.push_back(grouped[i + q]);
+      wd.entries += steps * S;
+      i += c;
     }
     for (int32_t r : longr) {
       const int64_t l = L_of(r);
@@ -121,10 +141,10 @@ BatchHost* batch_build(int n, const int64_t* n_rows, const int64_t* n_cols, cons
       wd.long_nchunks.push_back((int32_t)nch);
       for (int64_t c = 0; c < nch; ++c) {
         const int64_t clen = std::min<int64_t>(chunk, l - c * chunk);
-        const int64_t steps = (clen + G - 1) / G;
+        const int64_t steps = (clen + S - 1) / S;
         wd.tasks.push_back(
-            SlicedTask{(int32_t)wd.entries, (int32_t)(wd.chunks + c), (int32_t)steps, meta(kSlicedChunk, 1)});
-        wd.entries += steps * G;
+            SlicedTask{(int32_t)wd.entries, (int32_t)(wd.chunks + c), (int32_t)steps, meta(kSlicedChunk, 0, 1)});
+        wd.entries += steps * S;
       }
       wd.chunks += nch;
     }
@@ -188,15 +208,17 @@ BatchHost* batch_build(int n, const int64_t* n_rows, const int64_t* n_cols, cons
     int64_t chunk_in_row = 0;
     for (size_t ti = 0; ti < wd.tasks.size(); ++ti) {
       SlicedTask t = wd.tasks[ti];
-      const int kind = t.meta & 15, nrows = t.meta >> 8;
+      const int kind = t.meta & 15, vwl = (t.meta >> 4) & 15, nrows = t.meta >> 8;
       if (kind != kSlicedZero) t.base += (int32_t)off_e[w];
       t.row_base += (int32_t)(kind == kSlicedChunk ? off_c[w] : off_r[w]);
       h->tasks[(size_t)(off_t[w] + (int64_t)ti)] = t;
       if (kind == kSlicedZero) continue;
-      const int64_t span = (int64_t)t.steps * G;
+      const int64_t span = (int64_t)t.steps * S;
       double* vdst = h->val.get() + t.base;
       int32_t* cdst = h->col.get() + t.base;
       if (kind == kSlicedRows) {
+        const int64_t V = (int64_t)1 << vwl;
+        const int G = S >> vwl;
         for (int g = 0; g < G; ++g) {
           const int32_t r = h->rowid[(size_t)(t.row_base + (g < nrows ? g : 0))];
           const int32_t* cp;
@@ -206,8 +228,8 @@ BatchHost* batch_build(int n, const int64_t* n_rows, const int64_t* n_cols, cons
           row(r, &cp, &vp, &len, &coff);
           if (g >= nrows) len = 0;
           const int32_t padc = coff + cp[(g < nrows ? len : 1) - 1];
-          for (int64_t j = 0; j < t.steps; ++j) {
-            const int64_t pos = j * G + g;
+          for (int64_t j = 0; j < t.steps * V; ++j) {
+            const int64_t pos = (j / V) * S + g * V + (j % V);
             if (j < len) {
               cdst[pos] = coff + cp[j];
               vdst[pos] = vp[j];

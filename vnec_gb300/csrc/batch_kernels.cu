@@ -1,27 +1,35 @@
 // Batched multi-right-hand-side SpMV kernel (batch.h): one persistent launch
 // over the task list of the block-diagonal concatenation of the batch.
 //
-// Lane l of a warp serves task slot g = l / L and right-hand sides
-// [sub * R, sub * R + R) with sub = l % L, R = k / L.  At every step the warp
-// reads the G = 32 / L (value, column) pairs of one step (lanes of a slot read
-// the same pair, a broadcast) and each lane gathers R consecutive values of
-// row `column` of X with 16-byte vector loads, so the L lanes of a slot read
-// the whole k-wide X row.  No cross-lane reduction is needed for ROWS tasks:
-// every lane owns its own outputs.  CHUNK tasks (pieces of rows longer than
-// the grouping limit) spread entries over the G slots; the slots are summed
-// with xor-shuffles in FP64 and the last chunk of a row to arrive (an arrival
-// counter per long row, reset by that chunk) adds the row's chunk sums in
-// chunk order, so no second kernel is needed.
+// Lane l of a warp serves right-hand sides [sub * R, sub * R + R) with
+// sub = l % L, R = k / L, and slot l / L of the S = 32 / L (value, column)
+// slots the warp reads at every step (lanes of a slot read the same pair, a
+// broadcast).  A ROWS task holds G = S / V rows, V = 2^vwl slots per row:
+// entry j of row g sits at base + (j / V) * S + g * V + j % V, each lane
+// gathers R consecutive values of row `column` of X with 16-byte vector loads
+// (so the L lanes of a slot read the whole k-wide X row), and the V slots of a
+// row are summed with xor-shuffles.  CHUNK tasks (pieces of rows longer than
+// the grouping limit) use all S slots for one row; their sums go to chunk_sum
+// and the last chunk of a row to arrive (an arrival counter per long row,
+// reset by that chunk) adds the row's chunk sums in chunk order, so no second
+// kernel is needed.
 //
-// Precision forms: FP64 (FP64 values, X and FMA) and FP32 (FP32 values, X
-// rounded to FP32 once per call by a preceding kernel, FP32 products and
-// per-lane accumulation; chunk, slot and long-row sums in FP64).
+// Arithmetic forms (codecs):
+//   FP64 — FP64 values, X and FMA;
+//   FP32 — FP32 values, X rounded to FP32 once per call by a preceding kernel,
+//          FP32 products and per-lane accumulation; slot, chunk and long-row
+//          sums in FP64;
+//   DF32 — values stored as FP32 (hi, lo) truncation-split pairs, X split once
+//          per call; Dekker products and TwoSum accumulation on the FP32 pipe
+//          (FP64-level accuracy), FP64 slot/chunk sums.  When the split kernel
+//          flags an X value outside the split range, the same launch computes
+//          in FP64 (value = hi + lo, FP64 X).
 
 #include <cuda_runtime.h>
 
 #include <algorithm>
 #include <cstdint>
-#include <mutex>
+#include <cstring>
 
 #include "batch.h"
 #include "common.h"
@@ -42,36 +50,29 @@ struct BatchArgs {
   const int32_t* chunk_long;
   double* chunk_sum;
   int* chunk_count;
-  const void* x;
+  const void* x;       // X in the codec's element type
+  const double* x64;   // DF32: the FP64 X (guard path)
+  const int* flag;     // DF32: X outside the split range this call
   double* y;
   int klog2;  // k = 1 << klog2
   int llog2;  // lanes per slot L = 1 << llog2
 };
 
-// R consecutive values of X (16-byte vector loads where R allows).
-template <typename V, int R> __device__ __forceinline__ void load_x(const V* p, V (&v)[R]) {
-  if constexpr (R == 1) {
-    v[0] = __ldg(p);
-  } else if constexpr (sizeof(V) == 8) {
+// R consecutive elements of type T at p (16-, 8- or 4-byte vector loads).
+template <typename T, int R> __device__ __forceinline__ void load_vec(const T* p, T (&v)[R]) {
+  constexpr int bytes = R * (int)sizeof(T);
+  if constexpr (bytes >= 16) {
 #pragma unroll
-    for (int i = 0; i < R / 2; ++i) {
-      const double2 a = __ldg(reinterpret_cast<const double2*>(p) + i);
-      v[2 * i] = a.x;
-      v[2 * i + 1] = a.y;
+    for (int i = 0; i < bytes / 16; ++i) {
+      const int4 q = __ldg(reinterpret_cast<const int4*>(p) + i);
+      memcpy(reinterpret_cast<char*>(v) + 16 * i, &q, 16);
     }
-  } else if constexpr (R == 2) {
-    const float2 a = __ldg(reinterpret_cast<const float2*>(p));
-    v[0] = a.x;
-    v[1] = a.y;
+  } else if constexpr (bytes == 8) {
+    const int2 q = __ldg(reinterpret_cast<const int2*>(p));
+    memcpy(v, &q, 8);
   } else {
-#pragma unroll
-    for (int i = 0; i < R / 4; ++i) {
-      const float4 a = __ldg(reinterpret_cast<const float4*>(p) + i);
-      v[4 * i] = a.x;
-      v[4 * i + 1] = a.y;
-      v[4 * i + 2] = a.z;
-      v[4 * i + 3] = a.w;
-    }
+    const int q = __ldg(reinterpret_cast<const int*>(p));
+    memcpy(v, &q, 4);
   }
 }
 
@@ -84,64 +85,122 @@ template <int R> __device__ __forceinline__ void store_y(double* p, const double
   }
 }
 
-__device__ __forceinline__ double fmav(double a, double b, double c) { return fma(a, b, c); }
-__device__ __forceinline__ float fmav(float a, float b, float c) { return fmaf(a, b, c); }
+struct CodecF64 {
+  using V = double;
+  using X = double;
+  struct A {
+    double s;
+  };
+  __device__ static A zero() { return A{0.0}; }
+  __device__ static void mac(A& a, V v, X x) { a.s = fma(v, x, a.s); }
+  __device__ static double out(const A& a) { return a.s; }
+};
 
-template <typename V, int R, int U>
-__global__ void __launch_bounds__(256) batch_kernel(const BatchArgs a) {
+struct CodecF32 {
+  using V = float;
+  using X = float;
+  struct A {
+    float s;
+  };
+  __device__ static A zero() { return A{0.f}; }
+  __device__ static void mac(A& a, V v, X x) { a.s = fmaf(v, x, a.s); }
+  __device__ static double out(const A& a) { return static_cast<double>(a.s); }
+};
+
+// Double-float: value (hi, lo) times x (hi, lo), Dekker product with FMA,
+// TwoSum into (s, c).
+struct CodecDF32 {
+  using V = float2;
+  using X = float2;
+  struct A {
+    float s, c;
+  };
+  __device__ static A zero() { return A{0.f, 0.f}; }
+  __device__ static void mac(A& a, V v, X x) {
+    const float p = __fmul_rn(v.x, x.x);
+    const float e = fmaf(v.x, x.x, -p);
+    const float q = fmaf(v.x, x.y, fmaf(v.y, x.x, e));
+    const float t = __fadd_rn(a.s, p);
+    const float bb = __fsub_rn(t, a.s);
+    const float r = __fadd_rn(__fsub_rn(a.s, __fsub_rn(t, bb)), __fsub_rn(p, bb));
+    a.s = t;
+    a.c = __fadd_rn(a.c, __fadd_rn(r, q));
+  }
+  __device__ static double out(const A& a) { return static_cast<double>(a.s) + static_cast<double>(a.c); }
+};
+
+// FP64 from split values and FP64 X: the guard path of DF32 plans.
+struct CodecDF32Guard {
+  using V = float2;
+  using X = double;
+  struct A {
+    double s;
+  };
+  __device__ static A zero() { return A{0.0}; }
+  __device__ static void mac(A& a, V v, X x) {
+    a.s = fma(static_cast<double>(v.x) + static_cast<double>(v.y), x, a.s);
+  }
+  __device__ static double out(const A& a) { return a.s; }
+};
+
+template <class Cd, int R, int U>
+__device__ __forceinline__ void run_tasks(const BatchArgs& a, const typename Cd::X* __restrict__ x) {
+  using V = typename Cd::V;
+  using X = typename Cd::X;
   const int lane = threadIdx.x & 31;
   const int k = 1 << a.klog2;
-  const int G = 32 >> a.llog2;
-  const int g = lane >> a.llog2, sub = lane & ((1 << a.llog2) - 1);
+  const int S = 32 >> a.llog2;  // slots per step
+  const int slot = lane >> a.llog2, sub = lane & ((1 << a.llog2) - 1);
   const long long nw = (long long)gridDim.x * (blockDim.x >> 5);
   const V* __restrict__ val = static_cast<const V*>(a.val);
-  const V* __restrict__ xs = static_cast<const V*>(a.x) + sub * R;
+  const X* __restrict__ xs = x + sub * R;
   for (long long t = (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); t < a.num_tasks; t += nw) {
     const int4 raw = __ldg(a.tasks + t);
-    const int base = raw.x, row_base = raw.y, steps = raw.z, kind = raw.w & 15, nrows = raw.w >> 8;
+    const int base = raw.x, row_base = raw.y, steps = raw.z, kind = raw.w & 15, vwl = (raw.w >> 4) & 15,
+              nrows = raw.w >> 8;
     if (kind == kSlicedZero) {
       for (int i = lane; i < (nrows << a.klog2); i += 32)
         a.y[((size_t)__ldg(a.rowid + row_base + (i >> a.klog2)) << a.klog2) + (i & (k - 1))] = 0.0;
       continue;
     }
-    const V* vp = val + base + g;
-    const int32_t* cp = a.col + base + g;
-    V acc[R];
+    const V* vp = val + base + slot;
+    const int32_t* cp = a.col + base + slot;
+    typename Cd::A acc[R];
 #pragma unroll
-    for (int r = 0; r < R; ++r) acc[r] = V(0);
+    for (int r = 0; r < R; ++r) acc[r] = Cd::zero();
     int s = 0;
     for (; s + U <= steps; s += U) {
       int c[U];
       V v[U];
 #pragma unroll
       for (int u = 0; u < U; ++u) {
-        c[u] = __ldcs(cp + (s + u) * G);
-        v[u] = __ldcs(vp + (s + u) * G);
+        c[u] = __ldcs(cp + (s + u) * S);
+        v[u] = __ldcs(vp + (s + u) * S);
       }
-      V xv[U][R];
+      X xv[U][R];
 #pragma unroll
-      for (int u = 0; u < U; ++u) load_x<V, R>(xs + ((size_t)c[u] << a.klog2), xv[u]);
+      for (int u = 0; u < U; ++u) load_vec<X, R>(xs + ((size_t)c[u] << a.klog2), xv[u]);
 #pragma unroll
       for (int u = 0; u < U; ++u)
 #pragma unroll
-        for (int r = 0; r < R; ++r) acc[r] = fmav(v[u], xv[u][r], acc[r]);
+        for (int r = 0; r < R; ++r) Cd::mac(acc[r], v[u], xv[u][r]);
     }
     for (; s < steps; ++s) {
-      const int c = __ldcs(cp + s * G);
-      const V v = __ldcs(vp + s * G);
-      V xv[R];
-      load_x<V, R>(xs + ((size_t)c << a.klog2), xv);
+      const int c = __ldcs(cp + s * S);
+      const V v = __ldcs(vp + s * S);
+      X xv[R];
+      load_vec<X, R>(xs + ((size_t)c << a.klog2), xv);
 #pragma unroll
-      for (int r = 0; r < R; ++r) acc[r] = fmav(v, xv[r], acc[r]);
+      for (int r = 0; r < R; ++r) Cd::mac(acc[r], v, xv[r]);
     }
     double d[R];
 #pragma unroll
-    for (int r = 0; r < R; ++r) d[r] = static_cast<double>(acc[r]);
+    for (int r = 0; r < R; ++r) d[r] = Cd::out(acc[r]);
     if (kind == kSlicedChunk) {
       for (int off = 1 << a.llog2; off < 32; off <<= 1)
 #pragma unroll
         for (int r = 0; r < R; ++r) d[r] += __shfl_xor_sync(kFull, d[r], off);
-      if (g == 0) store_y<R>(a.chunk_sum + ((size_t)row_base << a.klog2) + sub * R, d);
+      if (slot == 0) store_y<R>(a.chunk_sum + ((size_t)row_base << a.klog2) + sub * R, d);
       __threadfence();
       __syncwarp();
       const int li = __ldg(a.chunk_long + row_base);
@@ -159,25 +218,48 @@ __global__ void __launch_bounds__(256) batch_kernel(const BatchArgs a) {
         }
         if (lane == 0) a.chunk_count[li] = 0;
       }
-    } else if (g < nrows) {
-      store_y<R>(a.y + ((size_t)__ldg(a.rowid + row_base + g) << a.klog2) + sub * R, d);
+    } else {
+      const int vspan = 1 << (a.llog2 + vwl);  // lanes of one row: L * V
+      for (int off = 1 << a.llog2; off < vspan; off <<= 1)
+#pragma unroll
+        for (int r = 0; r < R; ++r) d[r] += __shfl_xor_sync(kFull, d[r], off);
+      const int g = slot >> vwl;
+      if ((slot & ((1 << vwl) - 1)) == 0 && g < nrows)
+        store_y<R>(a.y + ((size_t)__ldg(a.rowid + row_base + g) << a.klog2) + sub * R, d);
     }
   }
 }
 
-template <typename V, int R> constexpr int unroll_for() { return R >= 4 ? 2 : 8 / R; }
+template <class Cd, int R, int U>
+__global__ void __launch_bounds__(256) batch_kernel(const BatchArgs a) {
+  run_tasks<Cd, R, U>(a, static_cast<const typename Cd::X*>(a.x));
+}
 
-template <typename V, int R> void* kernel_ptr() {
-  return reinterpret_cast<void*>(&batch_kernel<V, R, unroll_for<V, R>()>);
+template <int R, int U>
+__global__ void __launch_bounds__(256) batch_df32_kernel(const BatchArgs a) {
+  if (*reinterpret_cast<const volatile int*>(a.flag))
+    run_tasks<CodecDF32Guard, R, U>(a, a.x64);
+  else
+    run_tasks<CodecDF32, R, U>(a, static_cast<const float2*>(a.x));
+}
+
+template <int R> constexpr int unroll_for() { return R >= 4 ? 2 : 8 / R; }
+
+template <int R> void* kernel_for(int precision) {
+  constexpr int U = unroll_for<R>();
+  switch (precision) {
+    case kPrecFP32: return reinterpret_cast<void*>(&batch_kernel<CodecF32, R, U>);
+    case kPrecDF32: return reinterpret_cast<void*>(&batch_df32_kernel<R, U>);
+    default: return reinterpret_cast<void*>(&batch_kernel<CodecF64, R, U>);
+  }
 }
 
 void* pick_kernel(int precision, int r) {
-  const bool f32 = precision == kPrecFP32;
   switch (r) {
-    case 1: return f32 ? kernel_ptr<float, 1>() : kernel_ptr<double, 1>();
-    case 2: return f32 ? kernel_ptr<float, 2>() : kernel_ptr<double, 2>();
-    case 4: return f32 ? kernel_ptr<float, 4>() : kernel_ptr<double, 4>();
-    case 8: return f32 ? kernel_ptr<float, 8>() : kernel_ptr<double, 8>();
+    case 1: return kernel_for<1>(precision);
+    case 2: return kernel_for<2>(precision);
+    case 4: return kernel_for<4>(precision);
+    case 8: return kernel_for<8>(precision);
     default: return nullptr;
   }
 }
@@ -208,15 +290,20 @@ bool batch_spmm(const BatchMatrix& m, const double* X, double* Y, cudaStream_t s
   }
   const int R = m.k / m.lanes;
   const void* xin = X;
+  const long long nx = (long long)m.n_cols * m.k;
   if (m.precision == kPrecFP32) {
-    if (m.n_cols > 0 && !round_to_f32(X, m.xbuf, (long long)m.n_cols * m.k, s)) return false;
+    if (nx > 0 && !round_to_f32(X, static_cast<float*>(m.xbuf), nx, s)) return false;
+    xin = m.xbuf;
+  } else if (m.precision == kPrecDF32) {
+    if (!VNEC_CUDA(cudaMemsetAsync(m.flag, 0, sizeof(int), s))) return false;
+    if (nx > 0 && !split_to_df32(X, static_cast<float2*>(m.xbuf), nx, m.flag, s)) return false;
     xin = m.xbuf;
   }
   if (m.num_tasks == 0) return true;
   BatchArgs a;
   a.tasks = reinterpret_cast<const int4*>(m.tasks);
   a.num_tasks = m.num_tasks;
-  a.val = m.precision == kPrecFP32 ? static_cast<const void*>(m.val32) : static_cast<const void*>(m.val);
+  a.val = m.val;
   a.col = m.col;
   a.rowid = m.rowid;
   a.long_row = m.long_row;
@@ -225,6 +312,8 @@ bool batch_spmm(const BatchMatrix& m, const double* X, double* Y, cudaStream_t s
   a.chunk_sum = m.chunk_sum;
   a.chunk_count = m.chunk_count;
   a.x = xin;
+  a.x64 = X;
+  a.flag = m.flag;
   a.y = Y;
   a.klog2 = log2i(m.k);
   a.llog2 = log2i(m.lanes);

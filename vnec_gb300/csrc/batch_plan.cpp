@@ -22,13 +22,46 @@ namespace vnec {
 namespace {
 
 struct BatchDev {
-  DeviceBuffer tasks, val, val32, col, rowid, long_row, long_first, chunk_long, chunk_sum, chunk_count, xbuf;
+  DeviceBuffer tasks, val, col, rowid, long_row, long_first, chunk_long, chunk_sum, chunk_count, xbuf, flag;
   BatchMatrix m;
   int64_t bytes() const {
-    return (int64_t)(tasks.bytes + val.bytes + val32.bytes + col.bytes + rowid.bytes + long_row.bytes +
-                     long_first.bytes + chunk_long.bytes + chunk_sum.bytes + chunk_count.bytes + xbuf.bytes);
+    return (int64_t)(tasks.bytes + val.bytes + col.bytes + rowid.bytes + long_row.bytes + long_first.bytes +
+                     chunk_long.bytes + chunk_sum.bytes + chunk_count.bytes + xbuf.bytes + flag.bytes);
   }
 };
+
+// Truncation split of an FP64 value into FP32 hi (sign, exponent, top 23
+// mantissa bits) and lo (the remaining 29 bits, normalised and truncated to
+// 24): the host twin of the device split used for X, so that values and X of
+// the DF32 form are split the same way.  Needs a zero or |v| in [2^-40, 2^41).
+void split_df_host(double v, float* hi, float* lo) {
+  uint64_t b;
+  std::memcpy(&b, &v, 8);
+  const uint32_t sign = (uint32_t)(b >> 63) << 31;
+  const int e = (int)((b >> 52) & 0x7ff);
+  const uint64_t m = b & 0xFFFFFFFFFFFFFull;
+  if (e == 0 && m == 0) {
+    *hi = 0.f;
+    *lo = 0.f;
+    return;
+  }
+  const int E = e - 1023;
+  const uint32_t hb = sign | ((uint32_t)(E + 127) << 23) | (uint32_t)(m >> 29);
+  const uint32_t rem = (uint32_t)(m & 0x1FFFFFFFull);
+  const int msb = 31 - __builtin_clz(rem | 1u);
+  const uint32_t mant = msb > 23 ? (rem >> (msb - 23)) : (rem << (23 - msb));
+  const uint32_t lb = rem ? (sign | ((uint32_t)(E - 52 + msb + 127) << 23) | (mant & 0x7FFFFFu)) : 0u;
+  std::memcpy(hi, &hb, 4);
+  std::memcpy(lo, &lb, 4);
+}
+
+bool df32_range_ok(double v) {
+  if (v == 0.0) return true;
+  if (!std::isfinite(v)) return false;
+  int e = 0;
+  std::frexp(v, &e);
+  return e - 1 >= -40 && e - 1 <= 40;
+}
 
 bool up(DeviceBuffer& b, const void* src, size_t bytes, size_t extra = 64) {
   if (!b.alloc(bytes + extra)) return false;
@@ -47,12 +80,18 @@ bool upload_batch(const BatchHost* h, int k, int precision, int wpb, BatchDev* d
       !d->chunk_count.alloc(sizeof(int) * ((size_t)v.num_long + 16)) ||
       !VNEC_CUDA(cudaMemset(d->chunk_count.ptr, 0, d->chunk_count.bytes)))
     return false;
+  const size_t nx = std::max<size_t>((size_t)v.n_cols * k, 1);
   if (precision == kPrecFP32) {
     std::vector<float> f(ne);
 #pragma omp parallel for schedule(static)
     for (int64_t i = 0; i < (int64_t)ne; ++i) f[(size_t)i] = static_cast<float>(v.val[i]);
-    if (!up(d->val32, f.data(), sizeof(float) * ne, 0) ||
-        !d->xbuf.alloc(sizeof(float) * std::max<size_t>((size_t)v.n_cols * k, 1)))
+    if (!up(d->val, f.data(), sizeof(float) * ne, 0) || !d->xbuf.alloc(sizeof(float) * nx)) return false;
+  } else if (precision == kPrecDF32) {
+    std::vector<float> f(2 * ne);
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < (int64_t)ne; ++i) split_df_host(v.val[i], &f[2 * (size_t)i], &f[2 * (size_t)i + 1]);
+    if (!up(d->val, f.data(), sizeof(float) * 2 * ne, 0) || !d->xbuf.alloc(2 * sizeof(float) * nx) ||
+        !d->flag.alloc(16) || !VNEC_CUDA(cudaMemset(d->flag.ptr, 0, 16)))
       return false;
   } else if (!up(d->val, v.val, sizeof(double) * ne, 0)) {
     return false;
@@ -68,8 +107,8 @@ bool upload_batch(const BatchHost* h, int k, int precision, int wpb, BatchDev* d
   m.num_long = v.num_long;
   m.num_chunks = v.num_chunks;
   m.tasks = d->tasks.as<SlicedTask>();
-  m.val = d->val.as<double>();
-  m.val32 = d->val32.as<float>();
+  m.val = d->val.ptr;
+  m.flag = d->flag.as<int>();
   m.col = d->col.as<int32_t>();
   m.rowid = d->rowid.as<int32_t>();
   m.long_row = d->long_row.as<int32_t>();
@@ -77,7 +116,7 @@ bool upload_batch(const BatchHost* h, int k, int precision, int wpb, BatchDev* d
   m.chunk_long = d->chunk_long.as<int32_t>();
   m.chunk_sum = d->chunk_sum.as<double>();
   m.chunk_count = d->chunk_count.as<int>();
-  m.xbuf = d->xbuf.as<float>();
+  m.xbuf = d->xbuf.ptr;
   m.precision = precision;
   m.warps_per_block = wpb;
   m.grid = batch_grid(precision, k / v.lanes, wpb);
@@ -262,7 +301,7 @@ bool autotune(const BatchSource& s, int k, int precision, const SpB_VNEC_batch_o
   if (o->lanes > 0) lanes_c = {o->lanes};
   if (o->long_row_len > 0) long_c = {o->long_row_len};
   if (o->warps_per_block > 0) wpb_c = {o->warps_per_block};
-  const std::vector<int> pick = tune_sample(s, (int64_t)12 << 20);
+  const std::vector<int> pick = tune_sample(s, (int64_t)48 << 20);
   cudaStream_t st = nullptr;
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   if (!VNEC_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking)) || !VNEC_CUDA(cudaEventCreate(&e0)) ||
@@ -277,6 +316,7 @@ bool autotune(const BatchSource& s, int k, int precision, const SpB_VNEC_batch_o
       prm.long_len = ll;
       prm.chunk = o->chunk > 0 ? o->chunk : ll;
       if (o->window_rows > 0) prm.window_rows = o->window_rows;
+      if (o->max_steps > 0) prm.max_steps = o->max_steps;
       BatchHost* h = build_host(s, pick, k, prm);
       if (!h) continue;
       const BatchHostView hv = batch_view(h);
@@ -402,7 +442,7 @@ struct BatchPlan final : Plan {
   int launches_per_call() const override { return n_rows == 0 && precision != kPrecFP32 ? 0 : batch_launches(d.m); }
   int64_t device_bytes() const override { return d.bytes() + (int64_t)(dx.bytes + dy.bytes); }
   int64_t algorithmic_bytes() const override {
-    const int64_t vb = precision == kPrecFP32 ? 4 : 8;
+    const int64_t vb = precision == kPrecFP32 ? 4 : 8;  // DF32 stores (hi, lo) float pairs
     return nnz * (vb + 4) + (n_rows + (int64_t)row_off.size() - 1) * 4 + (n_cols + n_rows) * rhs * 8;
   }
   void describe(SpB_VNEC_info_ext* info) const override {
@@ -432,8 +472,8 @@ std::unique_ptr<Plan> build_batch(int n, const CsrView* mats, int k, const SpB_V
     set_error("batch: k must be 1, 2, 4, 8, 16 or 32");
     return nullptr;
   }
-  if (o.precision != kPrecFP64 && o.precision != kPrecFP32) {
-    set_error("batch: precision must be SpB_VNEC_PREC_FP64 or SpB_VNEC_PREC_FP32");
+  if (o.precision != kPrecFP64 && o.precision != kPrecFP32 && o.precision != kPrecDF32) {
+    set_error("batch: precision must be SpB_VNEC_PREC_FP64, SpB_VNEC_PREC_FP32 or SpB_VNEC_PREC_DF32");
     return nullptr;
   }
   if (o.lanes > 0 && !batch_supported(k, o.lanes)) {
@@ -444,7 +484,7 @@ std::unique_ptr<Plan> build_batch(int n, const CsrView* mats, int k, const SpB_V
     set_error("batch: warps_per_block must be 4 or 8");
     return nullptr;
   }
-  if (o.long_row_len < 0 || o.chunk < 0 || o.window_rows < 0) {
+  if (o.long_row_len < 0 || o.chunk < 0 || o.window_rows < 0 || o.max_steps < 0) {
     set_error("batch: negative option");
     return nullptr;
   }
@@ -471,6 +511,13 @@ std::unique_ptr<Plan> build_batch(int n, const CsrView* mats, int k, const SpB_V
       for (int64_t q = 0; q < v.nnz; ++q)
         if (!(std::fabs(a[q]) <= 3.4028234663852886e38)) {
           set_error("batch FP32 form: a value of matrix " + std::to_string(m) + " is not finite in FP32");
+          return nullptr;
+        }
+    } else if (o.precision == kPrecDF32) {
+      const double* a = static_cast<const double*>(v.val);
+      for (int64_t q = 0; q < v.nnz; ++q)
+        if (!df32_range_ok(a[q])) {
+          set_error("batch DF32 form: a value of matrix " + std::to_string(m) + " lies outside [2^-40, 2^41)");
           return nullptr;
         }
     }
@@ -516,6 +563,7 @@ std::unique_ptr<Plan> build_batch(int n, const CsrView* mats, int k, const SpB_V
   p->prm.long_len = choice.long_len;
   p->prm.chunk = o.chunk > 0 ? o.chunk : choice.long_len;
   if (o.window_rows > 0) p->prm.window_rows = o.window_rows;
+  if (o.max_steps > 0) p->prm.max_steps = o.max_steps;
   std::vector<int> all((size_t)n);
   for (int m = 0; m < n; ++m) all[(size_t)m] = m;
   BatchHost* h = build_host(src, all, k, p->prm);

@@ -137,6 +137,17 @@ bool same_key(const CacheKey& a, const CacheKey& b) {
 }
 
 std::unique_ptr<Plan> build_from_view(const CsrView& v, const SpB_VNEC_options_ext* opts) {
+  if (opts && opts->transpose) {
+    // y = A^T x: plan the transpose's CSR (the CSC of A) with the same options.
+    if (!validate_csr(v, false)) return nullptr;
+    CsrTranspose t;
+    if (!transpose_csr(v, &t)) return nullptr;
+    SpB_VNEC_options_ext o = *opts;
+    o.transpose = 0;
+    std::unique_ptr<Plan> p = build_from_view(t.view, &o);
+    if (p) p->transposed = true;
+    return p;
+  }
   int kernel = opts ? opts->kernel : SpB_VNEC_KERNEL_AUTO;
   switch (kernel) {
     case SpB_VNEC_KERNEL_AUTO:
@@ -152,6 +163,8 @@ std::unique_ptr<Plan> build_from_view(const CsrView& v, const SpB_VNEC_options_e
     case SpB_VNEC_KERNEL_SEARCH:
     case SpB_VNEC_KERNEL_RULE:
       return build_tuned(v, opts);
+    case SpB_VNEC_KERNEL_PUSH:
+      return build_push(v, opts);
     default:
       set_error("requested kernel is not available");
       return nullptr;
@@ -401,6 +414,27 @@ void* SpB_VNEC_batch_plan_matrices_ext(int n_mats, const SpB_Matrix* A, int k, c
       return nullptr;
     }
   return publish<VNEC_L>(build_batch(n_mats, views.data(), k, opts));
+}
+
+SpB_Info SpB_VNEC_spmspv_ext(void* plan, int64_t nnz_x, const int32_t* d_idx, const void* d_val, void* d_y,
+                             void* stream) {
+  clear_error();
+  Plan* p = find_plan(plan);
+  if (!p || nnz_x < 0 || (nnz_x > 0 && (!d_idx || !d_val)) || (p->n_rows > 0 && !d_y)) {
+    set_error("SpB_VNEC_spmspv_ext: invalid arguments");
+    return SpB_FAILURE;
+  }
+  return push_run_sparse(p, nnz_x, d_idx, d_val, d_y, static_cast<cudaStream_t>(stream)) ? SpB_SUCCESS : SpB_FAILURE;
+}
+
+SpB_Info SpB_VNEC_spmspv_host_ext(void* plan, int64_t nnz_x, const int32_t* idx, const void* val, void* y) {
+  clear_error();
+  Plan* p = find_plan(plan);
+  if (!p || nnz_x < 0 || (nnz_x > 0 && (!idx || !val)) || (p->n_rows > 0 && !y)) {
+    set_error("SpB_VNEC_spmspv_host_ext: invalid arguments");
+    return SpB_FAILURE;
+  }
+  return push_run_sparse_host(p, nnz_x, idx, val, y) ? SpB_SUCCESS : SpB_FAILURE;
 }
 
 SpB_Info SpB_VNEC_batch_offsets_ext(const void* plan, int64_t* row_offset, int64_t* col_offset) {

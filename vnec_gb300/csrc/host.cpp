@@ -173,6 +173,54 @@ void convert_cols(const CsrView& v, int32_t* out) {
   for (int64_t p = 0; p < v.nnz; ++p) out[p] = (int32_t)v.idx64[p];
 }
 
+bool transpose_csr(const CsrView& v, CsrTranspose* t) {
+  if (v.n_rows >= ((int64_t)1 << 31)) {
+    set_error("transpose: more than 2^31 rows");
+    return false;
+  }
+  const size_t vb = v.value_bytes();
+  t->row_ptr.assign((size_t)v.n_cols + 1, 0);
+  t->col.resize((size_t)std::max<int64_t>(v.nnz, 1));
+  t->val.resize((size_t)std::max<int64_t>(v.nnz, 1) * vb);
+  std::vector<int64_t> cursor((size_t)v.n_cols + 1, 0);
+  // Column counts, then positions reserved atomically; each transposed row is
+  // then sorted by original row so the result does not depend on thread timing.
+#pragma omp parallel for schedule(static)
+  for (int64_t p = 0; p < v.nnz; ++p) __atomic_fetch_add(&cursor[(size_t)v.col_at(p) + 1], 1, __ATOMIC_RELAXED);
+  for (int64_t c = 0; c < v.n_cols; ++c) cursor[(size_t)c + 1] += cursor[(size_t)c];
+  std::copy(cursor.begin(), cursor.end(), t->row_ptr.begin());
+  const unsigned char* src = static_cast<const unsigned char*>(v.val);
+#pragma omp parallel for schedule(dynamic, 1024)
+  for (int64_t r = 0; r < v.n_rows; ++r)
+    for (int64_t p = v.row_begin(r); p < v.row_begin(r + 1); ++p) {
+      const int64_t q = __atomic_fetch_add(&cursor[(size_t)v.col_at(p)], 1, __ATOMIC_RELAXED);
+      t->col[(size_t)q] = (int32_t)r;
+      std::memcpy(&t->val[(size_t)q * vb], src + (size_t)p * vb, vb);
+    }
+#pragma omp parallel for schedule(dynamic, 1024)
+  for (int64_t c = 0; c < v.n_cols; ++c) {
+    const int64_t b = t->row_ptr[(size_t)c], e = t->row_ptr[(size_t)c + 1];
+    if (e - b < 2) continue;
+    std::vector<std::pair<int32_t, int64_t>> order((size_t)(e - b));
+    for (int64_t q = b; q < e; ++q) order[(size_t)(q - b)] = {t->col[(size_t)q], q};
+    std::sort(order.begin(), order.end());
+    std::vector<unsigned char> vals((size_t)(e - b) * vb);
+    for (int64_t i = 0; i < e - b; ++i) std::memcpy(&vals[(size_t)i * vb], &t->val[(size_t)order[(size_t)i].second * vb], vb);
+    for (int64_t i = 0; i < e - b; ++i) t->col[(size_t)(b + i)] = order[(size_t)i].first;
+    std::memcpy(&t->val[(size_t)b * vb], vals.data(), vals.size());
+  }
+  t->view.type = v.type;
+  t->view.n_rows = v.n_cols;
+  t->view.n_cols = v.n_rows;
+  t->view.nnz = v.nnz;
+  t->view.ptr = t->row_ptr.data();
+  t->view.idx = t->col.data();
+  t->view.ptr64 = nullptr;
+  t->view.idx64 = nullptr;
+  t->view.val = t->val.data();
+  return true;
+}
+
 // ---------------------------------------------------------------------------
 // Plans and registry
 // ---------------------------------------------------------------------------

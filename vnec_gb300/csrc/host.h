@@ -34,12 +34,23 @@ bool view_from_arrays(SpB_Type type, int64_t n_rows, int64_t n_cols, const int64
 // Checks ptr[0]==0, monotone offsets, ptr[n]==nnz, 0<=col<n_cols (and, when
 // `need_sorted`, strictly increasing columns per row).
 bool validate_csr(const CsrView& v, bool need_sorted);
+// CSR of the transpose (rows = the input's columns, each row's columns in
+// increasing order) with a view over its arrays.
+struct CsrTranspose {
+  std::vector<int64_t> row_ptr;
+  std::vector<int32_t> col;
+  std::vector<unsigned char> val;
+  CsrView view;
+};
+bool transpose_csr(const CsrView& v, CsrTranspose* t);
 // Row ends (row_ptr[1..n]) as int32 or int64 and int32 columns.
 void convert_row_end(const CsrView& v, bool wide, void* out);
 void convert_cols(const CsrView& v, int32_t* out);
 
 // Kinds of plans this library builds.
-enum class PlanKind : int { kMergePath = 1, kWindowDense = 2, kWindowSliced = 3, kMixed = 4, kBatch = 5, kHybrid = 6 };
+enum class PlanKind : int {
+  kMergePath = 1, kWindowDense = 2, kWindowSliced = 3, kMixed = 4, kBatch = 5, kHybrid = 6, kPush = 7
+};
 
 // Base of every plan.  The reference-typed public struct handed to callers is
 // a separate calloc'd block registered against the plan (see registry below).
@@ -50,6 +61,7 @@ struct Plan {
   int rhs = 1;  // right-hand sides: x is n_cols x rhs, y is n_rows x rhs (row-major)
   int tune_config = -1;  // configuration index chosen by the tuner (tuner.h), -1 if built directly
   int tune_how = 0;      // SpB_VNEC_chosen_ext
+  bool transposed = false;  // the plan computes y = A^T x (built from A's transpose)
   int device = 0;
   cudaStream_t own_stream = nullptr;
   DeviceBuffer dx, dy;  // staging for host-vector calls
@@ -90,6 +102,10 @@ std::unique_ptr<Plan> build_dense(const CsrView& v, const SpB_VNEC_options_ext* 
 std::unique_ptr<Plan> build_hybrid(const CsrView& v, const SpB_VNEC_options_ext* opts);
 // Plans of kernel LEARNED / SEARCH / RULE (tuner.cpp).
 std::unique_ptr<Plan> build_tuned(const CsrView& v, const SpB_VNEC_options_ext* opts);
+// Push plans (SpMSpV, push_plan.cpp) and their sparse-x calls.
+std::unique_ptr<Plan> build_push(const CsrView& v, const SpB_VNEC_options_ext* opts);
+bool push_run_sparse(Plan* p, long long nx, const int32_t* d_idx, const void* d_val, void* d_y, cudaStream_t s);
+bool push_run_sparse_host(Plan* p, long long nx, const int32_t* idx, const void* val, void* y);
 // Batched multi-right-hand-side plan over n CSR matrices (all FP64).
 std::unique_ptr<Plan> build_batch(int n, const CsrView* mats, int k, const SpB_VNEC_batch_options_ext* opts);
 // Row and column offsets of each matrix in a batch plan's concatenation (n + 1 each).

@@ -97,6 +97,9 @@ bool sliced_mixed_spmv(const SlicedMatrix& m, const SlicedMixed& mx, const doubl
 bool sliced_guard_f64(const SlicedMatrix& m, const double* x, double* y, const int* flag, cudaStream_t s);
 // FP64 -> FP32 round-to-nearest-even of n values on stream s (one launch).
 bool round_to_f32(const double* x, float* x32, long long n, cudaStream_t s);
+// Truncation split of n FP64 values into FP32 (hi, lo) pairs; sets *flag when a
+// nonzero value lies outside [2^-40, 2^41) (the caller clears it).
+bool split_to_df32(const double* x, float2* xs, long long n, int* flag, cudaStream_t s);
 inline int sliced_mixed_launches(const SlicedMatrix& m, int precision) {
   return 2 + (precision == kPrecDF32 ? 1 : 0) + (m.num_long > 0 || precision == kPrecDF32 ? 1 : 0) +
          (precision == kPrecDF32 && m.hot > 0 ? 1 : 0);

@@ -307,6 +307,14 @@ bool sliced_mixed_spmv(const SlicedMatrix& m, const SlicedMixed& mx, const doubl
   return true;
 }
 
+bool split_to_df32(const double* x, float2* xs, long long n, int* flag, cudaStream_t s) {
+  if (n <= 0) return true;
+  const int tb = 256;
+  const int grid = (int)std::min<long long>((n + tb - 1) / tb, 152LL * 16);
+  x_split_kernel<<<grid, tb, 0, s>>>(x, xs, n, flag, nullptr, 0);
+  return VNEC_CUDA(cudaGetLastError());
+}
+
 bool round_to_f32(const double* x, float* x32, long long n, cudaStream_t s) {
   if (n <= 0) return true;
   const int tb = 256;
