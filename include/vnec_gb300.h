@@ -102,7 +102,7 @@ const char *SpB_VNEC_last_error_ext(void);
 
 /* Plan construction options (zero-initialise for defaults). */
 typedef enum {
-  SpB_VNEC_KERNEL_AUTO = 0,
+  SpB_VNEC_KERNEL_AUTO = 0, /* LEARNED when the library carries a trained model, else RULE */
   SpB_VNEC_KERNEL_L = 1, /* merge-path CSR */
   SpB_VNEC_KERNEL_D = 2, /* windowed dense blocks */
   SpB_VNEC_KERNEL_S = 3, /* windowed sliced rows */
@@ -185,6 +185,13 @@ void SpB_VNEC_forget_ext(const SpB_Matrix A);
  * cudaStream_t; NULL = legacy default stream) without synchronising.  Value
  * type of x and y is the plan's (FP64 or FP32). */
 SpB_Info SpB_mxv_device_ext(void *plan, const void *d_x, void *d_y, void *stream);
+
+/* y := alpha * (A x) + beta * z + gamma on device vectors (iterative
+ * solvers and graph analytics keep x and y on the GPU; the output transform
+ * is fused into the sliced kernel's stores, an elementwise pass elsewhere).
+ * z may be NULL (beta ignored) or equal to d_y (y := alpha A x + beta y). */
+SpB_Info SpB_mxv_axpby_ext(void *plan, const void *d_x, void *d_y, double alpha, double beta, const void *d_z,
+                           double gamma, void *stream);
 
 /* y := A x with host x and y (the SpB_mxv data path without SpB_Vector). */
 SpB_Info SpB_mxv_host_ext(void *plan, const void *h_x, void *h_y);

@@ -123,6 +123,8 @@ def lib() -> C.CDLL:
     L.SpB_VNEC_forget_ext.restype = None
     L.SpB_mxv_device_ext.argtypes = [_vp, _vp, _vp, _vp]
     L.SpB_mxv_device_ext.restype = C.c_int
+    L.SpB_mxv_axpby_ext.argtypes = [_vp, _vp, _vp, C.c_double, C.c_double, _vp, C.c_double, _vp]
+    L.SpB_mxv_axpby_ext.restype = C.c_int
     L.SpB_mxv_host_ext.argtypes = [_vp, _vp, _vp]
     L.SpB_mxv_host_ext.restype = C.c_int
     L.SpB_VNEC_plan_info_ext.argtypes = [_vp, C.POINTER(Info)]
@@ -388,6 +390,12 @@ class Plan:
     def mxv_device(self, d_x: int, d_y: int, stream: int = 0) -> None:
         """y = A x for device pointers (e.g. torch tensor data_ptr()) on a CUDA stream."""
         _check(lib().SpB_mxv_device_ext(self.h, d_x, d_y, stream or None) == SpB_SUCCESS, "SpB_mxv_device_ext")
+
+    def mxv_axpby(self, d_x: int, d_y: int, alpha: float = 1.0, beta: float = 0.0, d_z: int = 0,
+                  gamma: float = 0.0, stream: int = 0) -> None:
+        """y = alpha * A x + beta * z + gamma on device pointers (z may be y)."""
+        _check(lib().SpB_mxv_axpby_ext(self.h, d_x, d_y, alpha, beta, d_z or None, gamma, stream or None)
+               == SpB_SUCCESS, "SpB_mxv_axpby_ext")
 
     def mxv_host(self, x: np.ndarray, y: np.ndarray | None = None) -> np.ndarray:
         inf_rows = self.info().n_rows

@@ -10,6 +10,7 @@
 #include <unordered_map>
 
 #include "host.h"
+#include "tuner.h"
 
 using namespace vnec;
 
@@ -150,7 +151,16 @@ std::unique_ptr<Plan> build_from_view(const CsrView& v, const SpB_VNEC_options_e
   }
   int kernel = opts ? opts->kernel : SpB_VNEC_KERNEL_AUTO;
   switch (kernel) {
-    case SpB_VNEC_KERNEL_AUTO:
+    case SpB_VNEC_KERNEL_AUTO: {
+      // The learned selection when the library carries a trained model (it
+      // falls back to the exhaustive search for matrices outside its training
+      // range), otherwise the reference harness's rule.
+      SpB_VNEC_options_ext o;
+      std::memset(&o, 0, sizeof(o));
+      if (opts) o = *opts;
+      o.kernel = builtin_mlp_params() ? SpB_VNEC_KERNEL_LEARNED : SpB_VNEC_KERNEL_RULE;
+      return build_tuned(v, &o);
+    }
     case SpB_VNEC_KERNEL_L:
       return build_merge_path(v, opts);
     case SpB_VNEC_KERNEL_S:
@@ -492,6 +502,26 @@ SpB_Info SpB_mxv_device_ext(void* plan, const void* d_x, void* d_y, void* stream
     return SpB_FAILURE;
   }
   return p->run(d_x, d_y, static_cast<cudaStream_t>(stream)) ? SpB_SUCCESS : SpB_FAILURE;
+}
+
+SpB_Info SpB_mxv_axpby_ext(void* plan, const void* d_x, void* d_y, double alpha, double beta, const void* d_z,
+                           double gamma, void* stream) {
+  clear_error();
+  Plan* p = find_plan(plan);
+  if (!p) {
+    set_error("unknown plan");
+    return SpB_FAILURE;
+  }
+  if ((p->n_cols > 0 && !d_x) || (p->n_rows > 0 && !d_y)) {
+    set_error("x or y is NULL");
+    return SpB_FAILURE;
+  }
+  SlicedEpilogue e;
+  e.alpha = alpha;
+  e.beta = beta;
+  e.gamma = gamma;
+  e.z = beta != 0.0 ? d_z : nullptr;
+  return p->run_epilogue(d_x, d_y, e, static_cast<cudaStream_t>(stream)) ? SpB_SUCCESS : SpB_FAILURE;
 }
 
 SpB_Info SpB_mxv_host_ext(void* plan, const void* h_x, void* h_y) {

@@ -236,6 +236,19 @@ bool Plan::ensure_events() {
   return true;
 }
 
+bool Plan::run_epilogue(const void* d_x, void* d_y, const SlicedEpilogue& e, cudaStream_t s) {
+  SlicedEpilogue ee = e;
+  const size_t vb = type == SpB_FP64 ? 8 : 4;
+  const size_t ny = (size_t)n_rows * rhs;
+  if (e.z && e.z == d_y && e.beta != 0.0 && ny > 0) {
+    if (epi_scratch.bytes < vb * ny && !(epi_scratch.release(), epi_scratch.alloc(vb * ny))) return false;
+    if (!VNEC_CUDA(cudaMemcpyAsync(epi_scratch.ptr, d_y, vb * ny, cudaMemcpyDeviceToDevice, s))) return false;
+    ee.z = epi_scratch.ptr;
+  }
+  if (!run(d_x, d_y, s)) return false;
+  return apply_epilogue(d_y, (long long)ny, type == SpB_FP64, ee, s);
+}
+
 bool Plan::run_host(const void* h_x, void* h_y) {
   const size_t vb = type == SpB_FP64 ? 8 : 4;
   if (!own_stream && !VNEC_CUDA(cudaStreamCreateWithFlags(&own_stream, cudaStreamNonBlocking))) return false;

@@ -8,6 +8,7 @@
 #include <vector>
 
 #include "common.h"
+#include "sliced.h"
 #include "vnec_gb300.h"
 
 namespace vnec {
@@ -75,6 +76,11 @@ struct Plan {
   explicit Plan(PlanKind k) : kind(k) {}
   virtual ~Plan();
   virtual bool run(const void* d_x, void* d_y, cudaStream_t s) = 0;
+  // y := alpha * (A x) + beta * z + gamma.  Default: the SpMV, then an
+  // elementwise pass (z aliasing y is copied first); plans with a fused
+  // epilogue override it.
+  virtual bool run_epilogue(const void* d_x, void* d_y, const SlicedEpilogue& e, cudaStream_t s);
+  DeviceBuffer epi_scratch;
   virtual int launches_per_call() const = 0;
   virtual int64_t device_bytes() const = 0;
   // Algorithmic bytes moved by one call (roofline numerator).

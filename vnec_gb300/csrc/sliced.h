@@ -79,8 +79,17 @@ struct SlicedHostView {
 };
 SlicedHostView sliced_view(const SlicedHost* h);
 
+// Fused output transform: y := alpha * (A x) + beta * z + gamma (z may be
+// null, or alias y: each y entry is read and written by one thread).
+struct SlicedEpilogue {
+  double alpha = 1.0, beta = 0.0, gamma = 0.0;
+  const void* z = nullptr;
+};
+
 bool sliced_spmv(const SlicedMatrix& m, bool fp64, const void* x, void* y, cudaStream_t s,
-                 cudaEvent_t* events = nullptr);
+                 cudaEvent_t* events = nullptr, const SlicedEpilogue* epi = nullptr);
+// y[0..n) := alpha * y + beta * z + gamma (the unfused form of the epilogue).
+bool apply_epilogue(void* y, long long n, bool fp64, const SlicedEpilogue& e, cudaStream_t s);
 
 // Precision forms of the sliced format (sliced_mixed.cu).
 enum SlicedPrecision : int { kPrecFP64 = 0, kPrecFP32 = 1, kPrecBF16 = 2, kPrecDF32 = 3 };

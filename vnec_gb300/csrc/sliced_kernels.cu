@@ -181,12 +181,26 @@ __device__ __forceinline__ const V* x_at(const V* __restrict__ x, const V* __res
   else return x + c;
 }
 
-template <typename V, int U, int H, bool HOT = false>
+// Output of row `row`: the sum, or alpha * sum + beta * z[row] + gamma.
+// z is not restrict-qualified: it may alias y (the thread reads z[row] before
+// it writes y[row], and no other thread touches that entry).
+template <bool EPI, typename V>
+__device__ __forceinline__ V epi_out(V acc, int row, const SlicedEpilogue& ep) {
+  if constexpr (EPI) {
+    double r = fma(ep.alpha, static_cast<double>(acc), ep.gamma);
+    if (ep.z) r = fma(ep.beta, static_cast<double>(static_cast<const V*>(ep.z)[row]), r);
+    return static_cast<V>(r);
+  } else {
+    return acc;
+  }
+}
+
+template <typename V, int U, int H, bool HOT = false, bool EPI = false>
 __global__ void __launch_bounds__(kWarpsPerBlock * 32)
 sliced_kernel(const SlicedTask* __restrict__ tasks, long long num_tasks, const V* __restrict__ val,
               const int32_t* __restrict__ col, const int32_t* __restrict__ rowid, const V* __restrict__ x,
-              V* __restrict__ y, V* __restrict__ chunk_sum, const int* __restrict__ guard = nullptr,
-              const V* __restrict__ xh = nullptr, int ncols = 0) {
+              V* y, V* __restrict__ chunk_sum, const int* __restrict__ guard = nullptr,
+              const V* __restrict__ xh = nullptr, int ncols = 0, SlicedEpilogue ep = SlicedEpilogue()) {
   if (guard && *reinterpret_cast<const volatile int*>(guard) == 0) return;
   const long long w = ((long long)blockIdx.x * kWarpsPerBlock) + (threadIdx.x >> 5);
   const int lane = threadIdx.x & 31;
@@ -195,7 +209,10 @@ sliced_kernel(const SlicedTask* __restrict__ tasks, long long num_tasks, const V
   const int base = raw.x, row_base = raw.y, steps = raw.z, meta = raw.w;
   const int kind = meta & 15, vwl = (meta >> 4) & 15, nrows = meta >> 8;
   if (kind == kSlicedZero) {
-    if (lane < nrows) y[rowid[row_base + lane]] = V(0);
+    if (lane < nrows) {
+      const int row = rowid[row_base + lane];
+      y[row] = epi_out<EPI>(V(0), row, ep);
+    }
     return;
   }
   const V* vp = val + base + lane;
@@ -225,18 +242,32 @@ sliced_kernel(const SlicedTask* __restrict__ tasks, long long num_tasks, const V
     if (lane == 0) chunk_sum[row_base] = acc;
   } else {
     const int g = lane >> vwl;
-    if ((lane & ((1 << vwl) - 1)) == 0 && g < nrows) y[rowid[row_base + g]] = acc;
+    if ((lane & ((1 << vwl) - 1)) == 0 && g < nrows) {
+      const int row = rowid[row_base + g];
+      y[row] = epi_out<EPI>(acc, row, ep);
+    }
   }
 }
 
-template <typename V>
+template <typename V, bool EPI = false>
 __global__ void sliced_long_fixup(const int32_t* __restrict__ long_row, const int32_t* __restrict__ long_first,
-                                  long long num_long, const V* __restrict__ chunk_sum, V* __restrict__ y) {
+                                  long long num_long, const V* __restrict__ chunk_sum, V* y,
+                                  SlicedEpilogue ep = SlicedEpilogue()) {
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= num_long) return;
   V s = V(0);
   for (int c = long_first[i]; c < long_first[i + 1]; ++c) s += chunk_sum[c];
-  y[long_row[i]] = s;
+  const int row = long_row[i];
+  y[row] = epi_out<EPI>(s, row, ep);
+}
+
+template <typename V>
+__global__ void epilogue_kernel(V* y, long long n, SlicedEpilogue ep) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    double r = fma(ep.alpha, static_cast<double>(y[i]), ep.gamma);
+    if (ep.z) r = fma(ep.beta, static_cast<double>(static_cast<const V*>(ep.z)[i]), r);
+    y[i] = static_cast<V>(r);
+  }
 }
 
 template <typename V>
@@ -258,9 +289,10 @@ __global__ void gather_hot(const V* __restrict__ x, const int32_t* __restrict__ 
   if (i < n) xh[i] = __ldg(x + __ldg(hot_cols + i));
 }
 
-template <typename V, int U, int H, bool HOT>
-bool launch_main(const SlicedMatrix& m, const void* x, void* y, cudaStream_t s) {
-  auto kern = sliced_kernel<V, U, H, HOT>;
+template <typename V, int U, int H, bool HOT, bool EPI = false>
+bool launch_main(const SlicedMatrix& m, const void* x, void* y, cudaStream_t s,
+                 const SlicedEpilogue& ep = SlicedEpilogue()) {
+  auto kern = sliced_kernel<V, U, H, HOT, EPI>;
   static bool configured = false;
   if (!configured) {
     // No shared memory: give the whole unified L1/shared array to L1.
@@ -280,7 +312,7 @@ bool launch_main(const SlicedMatrix& m, const void* x, void* y, cudaStream_t s) 
   kern<<<(unsigned)grid, kWarpsPerBlock * 32, 0, s>>>(m.tasks, m.num_tasks, static_cast<const V*>(m.val), m.col,
                                                       m.rowid, static_cast<const V*>(x), static_cast<V*>(y),
                                                       static_cast<V*>(m.chunk_sum), nullptr,
-                                                      static_cast<const V*>(m.xhot), (int)m.n_cols);
+                                                      static_cast<const V*>(m.xhot), (int)m.n_cols, ep);
   return VNEC_CUDA(cudaGetLastError());
 }
 
@@ -310,19 +342,36 @@ bool launch_variant(const SlicedMatrix& m, const void* x, void* y, cudaStream_t 
 }
 
 template <typename V>
-bool launch(const SlicedMatrix& m, const void* x, void* y, cudaStream_t s, cudaEvent_t* ev) {
+bool launch(const SlicedMatrix& m, const void* x, void* y, cudaStream_t s, cudaEvent_t* ev,
+            const SlicedEpilogue* epi) {
   if (ev && !VNEC_CUDA(cudaEventRecord(ev[0], s))) return false;
+  // The fused epilogue runs in the default variant (unroll 12, default cache
+  // hints); dense-block plans apply it as a separate pass.
+  const bool fused = epi && m.vpe == 1;
   if (m.num_tasks > 0) {
-    const bool ok = m.vpe == 4 ? launch_dense<V>(m, x, y, s) : launch_variant<V>(m, x, y, s);
+    bool ok;
+    if (m.vpe == 4)
+      ok = launch_dense<V>(m, x, y, s);
+    else if (fused)
+      ok = m.hot > 0 ? launch_main<V, 12, 0, true, true>(m, x, y, s, *epi)
+                     : launch_main<V, 12, 0, false, true>(m, x, y, s, *epi);
+    else
+      ok = launch_variant<V>(m, x, y, s);
     if (!ok) return false;
   }
   if (ev && !VNEC_CUDA(cudaEventRecord(ev[1], s))) return false;
   if (m.num_long > 0) {
     const int b = 128;
-    sliced_long_fixup<V><<<(unsigned)((m.num_long + b - 1) / b), b, 0, s>>>(
-        m.long_row, m.long_first, m.num_long, static_cast<const V*>(m.chunk_sum), static_cast<V*>(y));
+    const unsigned g = (unsigned)((m.num_long + b - 1) / b);
+    if (fused)
+      sliced_long_fixup<V, true><<<g, b, 0, s>>>(m.long_row, m.long_first, m.num_long,
+                                                 static_cast<const V*>(m.chunk_sum), static_cast<V*>(y), *epi);
+    else
+      sliced_long_fixup<V><<<g, b, 0, s>>>(m.long_row, m.long_first, m.num_long, static_cast<const V*>(m.chunk_sum),
+                                           static_cast<V*>(y));
     if (!VNEC_CUDA(cudaGetLastError())) return false;
   }
+  if (epi && !fused && !apply_epilogue(y, m.n_rows, sizeof(V) == 8, *epi, s)) return false;
   if (ev && !VNEC_CUDA(cudaEventRecord(ev[2], s))) return false;
   return true;
 }
@@ -348,8 +397,20 @@ bool sliced_guard_f64(const SlicedMatrix& m, const double* x, double* y, const i
   return VNEC_CUDA(cudaGetLastError());
 }
 
-bool sliced_spmv(const SlicedMatrix& m, bool fp64, const void* x, void* y, cudaStream_t s, cudaEvent_t* ev) {
-  return fp64 ? launch<double>(m, x, y, s, ev) : launch<float>(m, x, y, s, ev);
+bool sliced_spmv(const SlicedMatrix& m, bool fp64, const void* x, void* y, cudaStream_t s, cudaEvent_t* ev,
+                 const SlicedEpilogue* epi) {
+  return fp64 ? launch<double>(m, x, y, s, ev, epi) : launch<float>(m, x, y, s, ev, epi);
+}
+
+bool apply_epilogue(void* y, long long n, bool fp64, const SlicedEpilogue& e, cudaStream_t s) {
+  if (n <= 0) return true;
+  const int tb = 256;
+  const unsigned grid = (unsigned)std::min<long long>((n + tb - 1) / tb, 152LL * 16);
+  if (fp64)
+    epilogue_kernel<double><<<grid, tb, 0, s>>>(static_cast<double*>(y), n, e);
+  else
+    epilogue_kernel<float><<<grid, tb, 0, s>>>(static_cast<float*>(y), n, e);
+  return VNEC_CUDA(cudaGetLastError());
 }
 
 }  // namespace vnec

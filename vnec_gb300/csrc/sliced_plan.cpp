@@ -35,6 +35,13 @@ struct SlicedPlan final : Plan {
     cudaEventElapsedTime(&ms[1], events[1], events[2]);
     return 2;
   }
+  bool run_epilogue(const void* d_x, void* d_y, const SlicedEpilogue& e, cudaStream_t s) override {
+    // Fused into the sliced kernel's (and long-row fix-up's) stores for the
+    // plain form; other forms use the elementwise pass.
+    if (mx.precision != kPrecFP64 || m.vpe != 1) return Plan::run_epilogue(d_x, d_y, e, s);
+    if (profiling && !ensure_events()) return false;
+    return sliced_spmv(m, type == SpB_FP64, d_x, d_y, s, profiling ? events : nullptr, &e);
+  }
   int launches_per_call() const override {
     if (n_rows == 0) return 0;
     return mx.precision != kPrecFP64 ? sliced_mixed_launches(m, mx.precision) : sliced_launches(m);
