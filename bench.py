@@ -439,7 +439,8 @@ def run_batch(args) -> None:
     n_rows = sum(m.n_rows for m in mats)
     n_cols = sum(m.n_cols for m in mats)
     ks = [int(v) for v in args.rhs.split(",")]
-    precs = [{"fp64": api.PREC_FP64, "fp32": api.PREC_FP32}[p] for p in args.batch_precision.split(",")]
+    precs = [{"fp64": api.PREC_FP64, "fp32": api.PREC_FP32, "df32": api.PREC_DF32}[p]
+             for p in args.batch_precision.split(",")]
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.int32, device=dev)
     stream = torch.cuda.Stream(device=dev)
     peak, peak_src = measured_peaks()
@@ -460,6 +461,7 @@ def run_batch(args) -> None:
             x = torch.from_numpy(xv).to(dev)
             y = torch.empty(n_rows * k, dtype=torch.float64, device=dev)
             B = batch_bytes(nnz, n_rows, n_cols, len(mats), k, 4 if prec == api.PREC_FP32 else 8)
+            pname = {api.PREC_FP64: "fp64", api.PREC_FP32: "fp32", api.PREC_DF32: "df32"}[prec]
             with torch.cuda.stream(stream):
                 for _ in range(args.warmup):
                     flush.fill_(1)
@@ -509,7 +511,7 @@ def run_batch(args) -> None:
             rel = np.concatenate(errs)
             cand, tms, best = plan.tuning()
             mean_ms = total / args.batch_steps
-            leg = {"k": k, "precision": "fp32" if prec == api.PREC_FP32 else "fp64",
+            leg = {"k": k, "precision": pname,
                    "gbs": round(value, 2), "ms_per_step": round(mean_ms, 4),
                    "hbm_frac": round(B / (mean_ms / 1e3) / 1e9 / peak, 4),
                    "fp64_tflops": round(2 * nnz * k / (mean_ms / 1e3) / 1e12, 4),
@@ -533,7 +535,8 @@ def run_batch(args) -> None:
     line = {
         "metric": METRIC, "value": leg["gbs"], "unit": "GB/s", "n_gpus": ws, "steps": args.batch_steps,
         "warmup": args.warmup, "ms_per_step": leg["ms_per_step"], "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64" if leg["precision"] == "fp64" else "f32 (fp64 reductions)",
+        "vs_baseline": None,
+        "dtype": {"fp64": "f64", "fp32": "f32 (fp64 reductions)", "df32": "f32 hi+lo (double-float)"}[leg["precision"]],
         "data": "synthetic (seeded generator, resident in HBM before timing)",
         "config": {"workload": "batch512_lognormal_" + leg["precision"] + f"_k{leg['k']}", "desc": BATCH_DESC,
                    "n_mats": len(mats), "n_rows": n_rows, "n_cols": n_cols, "nnz": nnz, "k": leg["k"],

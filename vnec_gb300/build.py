@@ -53,7 +53,8 @@ def build(verbose: bool = False, ptxas_info: bool = False) -> dict[str, str]:
     os.makedirs(OBJ, exist_ok=True)
     cuda = cuda_home()
     nvcc = os.path.join(cuda, "bin", "nvcc")
-    headers = glob.glob(os.path.join(CSRC, "*.h")) + glob.glob(os.path.join(INCLUDE, "*.h"))
+    headers = (glob.glob(os.path.join(CSRC, "*.h")) + glob.glob(os.path.join(CSRC, "*.cuh")) +
+               glob.glob(os.path.join(CSRC, "*.inc")) + glob.glob(os.path.join(INCLUDE, "*.h")))
     cu = sorted(glob.glob(os.path.join(CSRC, "*.cu")))
     cpp = sorted(p for p in glob.glob(os.path.join(CSRC, "*.cpp")) if not p.endswith("generators.cpp"))
     jobs = []

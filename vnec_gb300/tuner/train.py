@@ -87,7 +87,7 @@ def best_fixed_config(d: dict) -> int:
 
 def write_weights(path: str, params: np.ndarray, frange: np.ndarray, note: str) -> None:
     def arr(a):
-        vals = ", ".join(f"{float(v):.9g}f" for v in np.asarray(a, dtype=np.float32).ravel())
+        vals = ", ".join(f"{float(v):.9e}f" for v in np.asarray(a, dtype=np.float32).ravel())
         return "{" + vals + "}"
 
     with open(path, "w") as f:
