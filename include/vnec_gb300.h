@@ -345,7 +345,8 @@ typedef struct {
   int no_graph;        /* 1: launch the kernels directly on each call */
   int window_rows;     /* rows sorted by length within windows of this size (0: 65536) */
   int max_steps;       /* a row group spreads over enough slots to take at most this many steps (0: 32) */
-  int reserved[7];
+  int unroll;          /* load steps in flight per lane: 1 normal, 2 doubled; 0: tuned or normal */
+  int reserved[6];
 } SpB_VNEC_batch_options_ext;
 
 /* Plan from host CSR arrays per matrix: int64 row offsets (n_rows[m] + 1),
@@ -363,8 +364,9 @@ void *SpB_VNEC_batch_plan_matrices_ext(int n_mats, const SpB_Matrix *A, int k,
 SpB_Info SpB_VNEC_batch_offsets_ext(const void *plan, int64_t *row_offset, int64_t *col_offset);
 
 /* Autotuner result of a batch plan: candidates timed (0 if not tuned) and,
- * per candidate, {lanes, long_row_len, warps_per_block} and its median
- * milliseconds on the sample (up to `cap` entries); *best = chosen index. */
+ * per candidate, {lanes, long_row_len, warps_per_block, doubled unroll 0/1}
+ * and its median milliseconds on the sample (up to `cap` entries); *best =
+ * chosen index. */
 int SpB_VNEC_batch_tuning_ext(const void *plan, int *configs, float *ms, int cap, int *best);
 
 /* Per-kernel timing: when enabled, each SpMV of the plan records CUDA events

@@ -93,8 +93,8 @@ def test_batch_all_lanes(built, batch, k, precision):
     chunked rows (and the in-kernel long-row completion) are exercised."""
     from vnec_gb300 import api
 
-    for L in lanes_for(k):
-        p = api.BatchPlan(batch, k, lanes=L, long_row_len=64, precision=precision, max_steps=4)
+    for L, unroll in [(L, u) for L in lanes_for(k) for u in (1, 2)]:
+        p = api.BatchPlan(batch, k, lanes=L, long_row_len=64, precision=precision, max_steps=4, unroll=unroll)
         try:
             ro, co = p.offsets()
             X = _x(p, k)
@@ -206,11 +206,11 @@ def test_batch_autotune(built, batch, precision):
     p = api.BatchPlan(batch, k, autotune=True, precision=precision)
     try:
         cand, ms, best = p.tuning()
-        assert len(cand) == len(lanes_for(k)) * 3 * 2
+        assert len(cand) == len(lanes_for(k)) * 3 * 2 * 2
         assert 0 <= best < len(cand) and all(t > 0 for t in ms)
         assert ms[best] == min(ms)
         inf = p.info()
-        assert (inf.lanes, inf.long_row_len, inf.threads_per_block // 32) == cand[best]
+        assert (inf.lanes, inf.long_row_len, inf.threads_per_block // 32) == cand[best][:3]
         ro, co = p.offsets()
         X = _x(p, k)
         Yref, cond = oracle_batch(batch, X, k, co, ro)

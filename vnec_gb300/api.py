@@ -84,7 +84,7 @@ class BatchOptions(C.Structure):
 
     _fields_ = [("precision", C.c_int), ("lanes", C.c_int), ("long_row_len", C.c_int), ("chunk", C.c_int),
                 ("warps_per_block", C.c_int), ("autotune", C.c_int), ("no_graph", C.c_int),
-                ("window_rows", C.c_int), ("max_steps", C.c_int), ("reserved", C.c_int * 7)]
+                ("window_rows", C.c_int), ("max_steps", C.c_int), ("unroll", C.c_int), ("reserved", C.c_int * 6)]
 
 
 _vp = C.c_void_p
@@ -445,9 +445,9 @@ class Plan:
 
 def batch_options(precision: int = PREC_FP64, lanes: int = 0, long_row_len: int = 0, chunk: int = 0,
                   warps_per_block: int = 0, autotune: bool = False, graph: bool = True,
-                  window_rows: int = 0, max_steps: int = 0) -> BatchOptions:
+                  window_rows: int = 0, max_steps: int = 0, unroll: int = 0) -> BatchOptions:
     o = BatchOptions()
-    o.max_steps = max_steps
+    o.max_steps, o.unroll = max_steps, unroll
     o.precision, o.lanes, o.long_row_len, o.chunk = precision, lanes, long_row_len, chunk
     o.warps_per_block, o.autotune, o.no_graph, o.window_rows = warps_per_block, int(autotune), int(not graph), \
         window_rows
@@ -503,16 +503,17 @@ class BatchPlan(Plan):
         _check(lib().SpB_mxv_host_ext(self.h, x.ctypes.data, y.ctypes.data) == SpB_SUCCESS, "SpB_mxv_host_ext")
         return y
 
-    def tuning(self) -> tuple[list[tuple[int, int, int]], list[float], int]:
-        """Autotuner record: candidates (lanes, long_row_len, warps_per_block), median ms, chosen index."""
+    def tuning(self) -> tuple[list[tuple[int, int, int, int]], list[float], int]:
+        """Autotuner record: candidates (lanes, long_row_len, warps_per_block, deep unroll), median ms, chosen index."""
         cap = 256
-        cfg = (C.c_int * (3 * cap))()
+        cfg = (C.c_int * (4 * cap))()
         ms = (C.c_float * cap)()
         best = C.c_int(-1)
         n = lib().SpB_VNEC_batch_tuning_ext(self.h, cfg, ms, cap, C.byref(best))
         _check(n >= 0, "batch_tuning")
         n = min(n, cap)
-        return [(cfg[3 * i], cfg[3 * i + 1], cfg[3 * i + 2]) for i in range(n)], [ms[i] for i in range(n)], best.value
+        return ([(cfg[4 * i], cfg[4 * i + 1], cfg[4 * i + 2], cfg[4 * i + 3]) for i in range(n)],
+                [ms[i] for i in range(n)], best.value)
 
 
 # --- kernel selection ---------------------------------------------------------

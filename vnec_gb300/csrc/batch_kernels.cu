@@ -243,10 +243,11 @@ __global__ void __launch_bounds__(256) batch_df32_kernel(const BatchArgs a) {
     run_tasks<CodecDF32, R, U>(a, static_cast<const float2*>(a.x));
 }
 
-template <int R> constexpr int unroll_for() { return R >= 4 ? 2 : 8 / R; }
+// Steps in flight per lane: 8 / R (at least 2), doubled with `deep`.
+template <int R, bool DEEP> constexpr int unroll_for() { return (R >= 4 ? 2 : 8 / R) * (DEEP ? 2 : 1); }
 
-template <int R> void* kernel_for(int precision) {
-  constexpr int U = unroll_for<R>();
+template <int R, bool DEEP> void* kernel_for(int precision) {
+  constexpr int U = unroll_for<R, DEEP>();
   switch (precision) {
     case kPrecFP32: return reinterpret_cast<void*>(&batch_kernel<CodecF32, R, U>);
     case kPrecDF32: return reinterpret_cast<void*>(&batch_df32_kernel<R, U>);
@@ -254,12 +255,12 @@ template <int R> void* kernel_for(int precision) {
   }
 }
 
-void* pick_kernel(int precision, int r) {
+void* pick_kernel(int precision, int r, bool deep) {
   switch (r) {
-    case 1: return kernel_for<1>(precision);
-    case 2: return kernel_for<2>(precision);
-    case 4: return kernel_for<4>(precision);
-    case 8: return kernel_for<8>(precision);
+    case 1: return deep ? kernel_for<1, true>(precision) : kernel_for<1, false>(precision);
+    case 2: return deep ? kernel_for<2, true>(precision) : kernel_for<2, false>(precision);
+    case 4: return deep ? kernel_for<4, true>(precision) : kernel_for<4, false>(precision);
+    case 8: return deep ? kernel_for<8, true>(precision) : kernel_for<8, false>(precision);
     default: return nullptr;
   }
 }
@@ -272,8 +273,8 @@ int log2i(int v) {
 
 }  // namespace
 
-int batch_grid(int precision, int rhs_per_lane, int warps_per_block) {
-  void* fn = pick_kernel(precision, rhs_per_lane);
+int batch_grid(int precision, int rhs_per_lane, int warps_per_block, bool deep) {
+  void* fn = pick_kernel(precision, rhs_per_lane, deep);
   if (!fn || (warps_per_block != 4 && warps_per_block != 8)) return 0;
   int dev = 0, sms = 0, per_sm = 0;
   if (!VNEC_CUDA(cudaGetDevice(&dev)) ||
@@ -317,7 +318,7 @@ bool batch_spmm(const BatchMatrix& m, const double* X, double* Y, cudaStream_t s
   a.y = Y;
   a.klog2 = log2i(m.k);
   a.llog2 = log2i(m.lanes);
-  void* fn = pick_kernel(m.precision, R);
+  void* fn = pick_kernel(m.precision, R, m.deep);
   const int grid = (int)std::min<long long>(m.grid, std::max<long long>(1, (m.num_tasks + 7) / 8));
   void* args[] = {&a};
   return VNEC_CUDA(cudaLaunchKernel(fn, dim3((unsigned)grid), dim3((unsigned)(m.warps_per_block * 32)), args, 0, s));

@@ -68,7 +68,7 @@ bool up(DeviceBuffer& b, const void* src, size_t bytes, size_t extra = 64) {
   return bytes == 0 || VNEC_CUDA(cudaMemcpy(b.ptr, src, bytes, cudaMemcpyHostToDevice));
 }
 
-bool upload_batch(const BatchHost* h, int k, int precision, int wpb, BatchDev* d) {
+bool upload_batch(const BatchHost* h, int k, int precision, int wpb, bool deep, BatchDev* d) {
   const BatchHostView v = batch_view(h);
   const size_t ne = (size_t)v.entries + 64;
   if (!up(d->tasks, v.tasks, sizeof(SlicedTask) * (size_t)v.num_tasks) ||
@@ -119,7 +119,8 @@ bool upload_batch(const BatchHost* h, int k, int precision, int wpb, BatchDev* d
   m.xbuf = d->xbuf.ptr;
   m.precision = precision;
   m.warps_per_block = wpb;
-  m.grid = batch_grid(precision, k / v.lanes, wpb);
+  m.deep = deep;
+  m.grid = batch_grid(precision, k / v.lanes, wpb, deep);
   if (m.grid <= 0) {
     set_error("batch: no occupancy for the kernel");
     return false;
@@ -187,6 +188,7 @@ BatchHost* build_host(const BatchSource& s, const std::vector<int>& pick, int k,
 
 struct TuneChoice {
   int lanes = 0, long_len = 1024, wpb = 8;
+  int deep = 0;  // 1: twice the load steps in flight per lane
 };
 
 std::mutex g_tune_mu;
@@ -241,8 +243,10 @@ bool cache_file_lookup(const std::string& key, TuneChoice* c) {
   while (std::fgets(line, sizeof(line), f)) {
     char k[600];
     TuneChoice t;
-    if (std::sscanf(line, "{\"key\": \"%599[^\"]\", \"lanes\": %d, \"long_row_len\": %d, \"warps_per_block\": %d}", k,
-                    &t.lanes, &t.long_len, &t.wpb) == 4 &&
+    if (std::sscanf(line,
+                    "{\"key\": \"%599[^\"]\", \"lanes\": %d, \"long_row_len\": %d, \"warps_per_block\": %d, "
+                    "\"deep_unroll\": %d}",
+                    k, &t.lanes, &t.long_len, &t.wpb, &t.deep) == 5 &&
         key == k) {
       *c = t;
       found = true;
@@ -257,8 +261,10 @@ void cache_file_store(const std::string& key, const TuneChoice& c) {
   if (!path || !*path) return;
   FILE* f = std::fopen(path, "a");
   if (!f) return;
-  std::fprintf(f, "{\"key\": \"%s\", \"lanes\": %d, \"long_row_len\": %d, \"warps_per_block\": %d}\n", key.c_str(),
-               c.lanes, c.long_len, c.wpb);
+  std::fprintf(f,
+               "{\"key\": \"%s\", \"lanes\": %d, \"long_row_len\": %d, \"warps_per_block\": %d, "
+               "\"deep_unroll\": %d}\n",
+               key.c_str(), c.lanes, c.long_len, c.wpb, c.deep);
   std::fclose(f);
 }
 
@@ -295,12 +301,13 @@ float median_ms(std::vector<float> v) {
 }
 
 bool autotune(const BatchSource& s, int k, int precision, const SpB_VNEC_batch_options_ext* o, TuneRun* run) {
-  std::vector<int> lanes_c, long_c{256, 1024, 4096}, wpb_c{4, 8};
+  std::vector<int> lanes_c, long_c{256, 1024, 4096}, wpb_c{4, 8}, deep_c{0, 1};
   for (int L = 1; L <= 32; L <<= 1)
     if (batch_supported(k, L)) lanes_c.push_back(L);
   if (o->lanes > 0) lanes_c = {o->lanes};
   if (o->long_row_len > 0) long_c = {o->long_row_len};
   if (o->warps_per_block > 0) wpb_c = {o->warps_per_block};
+  if (o->unroll > 0) deep_c = {o->unroll - 1};
   const std::vector<int> pick = tune_sample(s, (int64_t)48 << 20);
   cudaStream_t st = nullptr;
   cudaEvent_t e0 = nullptr, e1 = nullptr;
@@ -329,20 +336,26 @@ bool autotune(const BatchSource& s, int k, int precision, const SpB_VNEC_batch_o
       }
       for (int wpb : wpb_c) {
         BatchDev d;
-        if (!upload_batch(h, k, precision, wpb, &d)) {
+        if (!upload_batch(h, k, precision, wpb, false, &d)) {
           ok = false;
           break;
         }
-        std::vector<float> t;
-        for (int rep = 0; rep < 7 && ok; ++rep) {
-          ok = VNEC_CUDA(cudaEventRecord(e0, st)) && batch_spmm(d.m, X.as<double>(), Y.as<double>(), st) &&
-               VNEC_CUDA(cudaEventRecord(e1, st)) && VNEC_CUDA(cudaEventSynchronize(e1));
-          float ms = 0.f;
-          if (ok && rep >= 2 && VNEC_CUDA(cudaEventElapsedTime(&ms, e0, e1))) t.push_back(ms);
+        for (int deep : deep_c) {
+          // The unroll changes only the kernel: same layout, new grid.
+          d.m.deep = deep != 0;
+          d.m.grid = batch_grid(precision, k / L, wpb, d.m.deep);
+          std::vector<float> t;
+          for (int rep = 0; rep < 7 && ok; ++rep) {
+            ok = VNEC_CUDA(cudaEventRecord(e0, st)) && batch_spmm(d.m, X.as<double>(), Y.as<double>(), st) &&
+                 VNEC_CUDA(cudaEventRecord(e1, st)) && VNEC_CUDA(cudaEventSynchronize(e1));
+            float ms = 0.f;
+            if (ok && rep >= 2 && VNEC_CUDA(cudaEventElapsedTime(&ms, e0, e1))) t.push_back(ms);
+          }
+          if (!ok) break;
+          run->cand.push_back(TuneChoice{L, ll, wpb, deep});
+          run->ms.push_back(median_ms(t));
         }
         if (!ok) break;
-        run->cand.push_back(TuneChoice{L, ll, wpb});
-        run->ms.push_back(median_ms(t));
       }
       batch_free(h);
       if (!ok) break;
@@ -484,7 +497,7 @@ std::unique_ptr<Plan> build_batch(int n, const CsrView* mats, int k, const SpB_V
     set_error("batch: warps_per_block must be 4 or 8");
     return nullptr;
   }
-  if (o.long_row_len < 0 || o.chunk < 0 || o.window_rows < 0 || o.max_steps < 0) {
+  if (o.long_row_len < 0 || o.chunk < 0 || o.window_rows < 0 || o.max_steps < 0 || o.unroll < 0 || o.unroll > 2) {
     set_error("batch: negative option");
     return nullptr;
   }
@@ -535,10 +548,11 @@ std::unique_ptr<Plan> build_batch(int n, const CsrView* mats, int k, const SpB_V
   if (o.lanes == 0 && k >= 8) choice.lanes = k / 4;  // four right-hand sides per lane
   if (o.long_row_len > 0) choice.long_len = o.long_row_len;
   if (o.warps_per_block > 0) choice.wpb = o.warps_per_block;
+  if (o.unroll > 0) choice.deep = o.unroll - 1;
   if (o.autotune) {
     const std::string key = tune_key(src, k, o.precision);
     bool hit = false;
-    if (o.lanes == 0 && o.long_row_len == 0 && o.warps_per_block == 0) {
+    if (o.lanes == 0 && o.long_row_len == 0 && o.warps_per_block == 0 && o.unroll == 0) {
       std::lock_guard<std::mutex> g(g_tune_mu);
       auto it = tune_cache().find(key);
       if (it != tune_cache().end()) {
@@ -552,7 +566,7 @@ std::unique_ptr<Plan> build_batch(int n, const CsrView* mats, int k, const SpB_V
     if (!hit) {
       if (!autotune(src, k, o.precision, &o, &p->tuning)) return nullptr;
       choice = p->tuning.cand[(size_t)p->tuning.best];
-      if (o.lanes == 0 && o.long_row_len == 0 && o.warps_per_block == 0) {
+      if (o.lanes == 0 && o.long_row_len == 0 && o.warps_per_block == 0 && o.unroll == 0) {
         std::lock_guard<std::mutex> g(g_tune_mu);
         tune_cache()[key] = choice;
         cache_file_store(key, choice);
@@ -571,7 +585,7 @@ std::unique_ptr<Plan> build_batch(int n, const CsrView* mats, int k, const SpB_V
     set_error("batch: more than 2^31 rows, columns or layout entries");
     return nullptr;
   }
-  const bool ok = upload_batch(h, k, o.precision, choice.wpb, &p->d);
+  const bool ok = upload_batch(h, k, o.precision, choice.wpb, choice.deep != 0, &p->d);
   batch_free(h);
   if (!ok) return nullptr;
   return p;
@@ -596,9 +610,10 @@ int batch_tuning(const Plan* p, int* configs, float* ms, int cap, int* best) {
   const int n = (int)t.cand.size();
   for (int i = 0; i < n && i < cap; ++i) {
     if (configs) {
-      configs[3 * i] = t.cand[(size_t)i].lanes;
-      configs[3 * i + 1] = t.cand[(size_t)i].long_len;
-      configs[3 * i + 2] = t.cand[(size_t)i].wpb;
+      configs[4 * i] = t.cand[(size_t)i].lanes;
+      configs[4 * i + 1] = t.cand[(size_t)i].long_len;
+      configs[4 * i + 2] = t.cand[(size_t)i].wpb;
+      configs[4 * i + 3] = t.cand[(size_t)i].deep;
     }
     if (ms) ms[i] = t.ms[(size_t)i];
   }
