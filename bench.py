@@ -150,6 +150,26 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(inside)}
 
 
+def replica_max(value: float, device=None) -> float:
+    """Max of `value` over the ranks of the default process group (the value
+    itself when no group is initialised); device: where the collective's
+    tensor lives (the rank's GPU for NCCL, the CPU for gloo)."""
+    import torch
+    import torch.distributed as dist
+
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return float(value)
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device or "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_throughput(bytes_per_step: int, steps: int, world: int, max_ms: float) -> float:
+    """Whole-job GB/s of `world` replicas that each ran `steps` steps, timed by
+    the slowest rank (weak scaling: every replica does the full workload)."""
+    return bytes_per_step * steps * world / (max_ms / 1e3) / 1e9
+
+
 def dist_env():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -314,12 +334,8 @@ def run_ours(args) -> None:
     barrier()
     w1 = time.time()
     step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
-    total_ms = float(np.sum(step_ms))
-    if ws > 1:
-        t = torch.tensor([total_ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(t.item())
-    value = B * args.steps * ws / (total_ms / 1e3) / 1e9
+    total_ms = replica_max(float(np.sum(step_ms)), dev)
+    value = replica_throughput(B, args.steps, ws, total_ms)
     y_dev = y.cpu().numpy()
 
     # ---- end to end through the C ABI with pinned host buffers --------------
@@ -340,12 +356,9 @@ def run_ours(args) -> None:
         e2e_s += time.perf_counter() - t0
     barrier()
     w2 = time.time()
-    if ws > 1:
-        t = torch.tensor([e2e_s], device=dev, dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_s = float(t.item())
+    e2e_s = replica_max(e2e_s, dev)
     clocks = sampler.stop(w0, w2)
-    e2e_value = B * e2e_steps * ws / e2e_s / 1e9
+    e2e_value = replica_throughput(B, e2e_steps, ws, e2e_s * 1e3)
     if not np.array_equal(hy_np, y_dev):
         raise RuntimeError("host-path and device-path results differ")
 
@@ -480,13 +493,9 @@ def run_batch(args) -> None:
                     ends[i].record(stream)
             torch.cuda.synchronize()
             ms = [a.elapsed_time(b) for a, b in zip(starts, ends)]
-            total = float(np.sum(ms))
-            if ws > 1:
-                t = torch.tensor([total], device=dev)
-                torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-                total = float(t.item())
+            total = replica_max(float(np.sum(ms)), dev)
             gpu_launches += args.batch_steps * info.launches_per_call
-            value = B * args.batch_steps * ws / (total / 1e3) / 1e9
+            value = replica_throughput(B, args.batch_steps, ws, total)
             # end to end: pinned host X / Y through SpB_mxv_host_ext
             hx = torch.from_numpy(xv).pin_memory()
             hy = torch.empty(n_rows * k, dtype=torch.float64).pin_memory()

@@ -3,6 +3,7 @@
 
 #include <cuda_runtime.h>
 #include <cstddef>
+#include <atomic>
 #include <cstdint>
 #include <string>
 
@@ -21,6 +22,22 @@ bool cuda_ok(cudaError_t e, const char* what);
 #define VNEC_CUDA(call) ::vnec::cuda_ok((call), #call)
 
 // Owning device allocation.
+// Runs `set` (a per-function CUDA attribute setting) once per device for one
+// call site: `mask` holds a bit per device ordinal already configured.
+template <class F>
+bool once_per_device(std::atomic<unsigned long long>& mask, F set) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) {
+    set_error("cudaGetDevice failed");
+    return false;
+  }
+  const unsigned long long bit = 1ull << (dev & 63);
+  if (mask.load(std::memory_order_acquire) & bit) return true;
+  if (!set()) return false;
+  mask.fetch_or(bit, std::memory_order_acq_rel);
+  return true;
+}
+
 struct DeviceBuffer {
   void* ptr = nullptr;
   size_t bytes = 0;

@@ -92,6 +92,7 @@ struct Plan {
   // Waits for the plan's work on `s` and reports device-side errors.
   virtual bool device_status(cudaStream_t s) { return VNEC_CUDA(cudaStreamSynchronize(s)); }
   bool run_host(const void* h_x, void* h_y);
+  std::mutex host_mu;  // serialises host-vector calls (they share dx, dy and own_stream)
 };
 
 // Registry: public handle pointer -> plan.

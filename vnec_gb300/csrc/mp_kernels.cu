@@ -185,12 +185,11 @@ bool launch_mp(const MpMatrix& m, const void* x, void* y, cudaStream_t s, cudaEv
   sh.tpb = TPB;
   sh.ipt = IPT;
   size_t smem = mp_smem_bytes(sh, sizeof(V));
-  static bool configured = false;  // per instantiation
-  if (!configured) {
-    if (!VNEC_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)))
-      return false;
-    configured = true;
-  }
+  static std::atomic<unsigned long long> configured{0};  // per instantiation, per device
+  if (!once_per_device(configured, [&] {
+        return VNEC_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+      }))
+    return false;
   if (m.num_tiles > 0x7fffffffLL) {
     set_error("merge-path: tile count exceeds the grid limit");
     return false;

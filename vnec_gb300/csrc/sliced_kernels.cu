@@ -293,12 +293,12 @@ template <typename V, int U, int H, bool HOT, bool EPI = false>
 bool launch_main(const SlicedMatrix& m, const void* x, void* y, cudaStream_t s,
                  const SlicedEpilogue& ep = SlicedEpilogue()) {
   auto kern = sliced_kernel<V, U, H, HOT, EPI>;
-  static bool configured = false;
-  if (!configured) {
-    // No shared memory: give the whole unified L1/shared array to L1.
-    if (!VNEC_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 0))) return false;
-    configured = true;
-  }
+  // No shared memory: give the whole unified L1/shared array to L1.
+  static std::atomic<unsigned long long> configured{0};  // per instantiation, per device
+  if (!once_per_device(configured, [&] {
+        return VNEC_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 0));
+      }))
+    return false;
   const long long grid = (m.num_tasks + kWarpsPerBlock - 1) / kWarpsPerBlock;
   if (grid > 0x7fffffffLL) {
     set_error("sliced: too many tasks for one launch");
