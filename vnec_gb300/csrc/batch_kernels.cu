@@ -86,6 +86,7 @@ template <int R> __device__ __forceinline__ void store_y(double* p, const double
 }
 
 struct CodecF64 {
+  static constexpr bool kPairReduce = false;
   using V = double;
   using X = double;
   struct A {
@@ -97,6 +98,7 @@ struct CodecF64 {
 };
 
 struct CodecF32 {
+  static constexpr bool kPairReduce = false;
   using V = float;
   using X = float;
   struct A {
@@ -110,11 +112,21 @@ struct CodecF32 {
 // Double-float: value (hi, lo) times x (hi, lo), Dekker product with FMA,
 // TwoSum into (s, c).
 struct CodecDF32 {
+  static constexpr bool kPairReduce = true;
   using V = float2;
   using X = float2;
   struct A {
     float s, c;
   };
+  // a += the (s, c) pair of the lane `off` away (TwoSum of the high parts).
+  __device__ static void add_shfl(A& a, int off) {
+    const float s2 = __shfl_xor_sync(0xffffffffu, a.s, off), c2 = __shfl_xor_sync(0xffffffffu, a.c, off);
+    const float t = __fadd_rn(a.s, s2);
+    const float bb = __fsub_rn(t, a.s);
+    const float e = __fadd_rn(__fsub_rn(a.s, __fsub_rn(t, bb)), __fsub_rn(s2, bb));
+    a.s = t;
+    a.c = __fadd_rn(a.c, __fadd_rn(c2, e));
+  }
   __device__ static A zero() { return A{0.f, 0.f}; }
   __device__ static void mac(A& a, V v, X x) {
     const float p = __fmul_rn(v.x, x.x);
@@ -131,6 +143,7 @@ struct CodecDF32 {
 
 // FP64 from split values and FP64 X: the guard path of DF32 plans.
 struct CodecDF32Guard {
+  static constexpr bool kPairReduce = false;
   using V = float2;
   using X = double;
   struct A {
@@ -193,13 +206,25 @@ __device__ __forceinline__ void run_tasks(const BatchArgs& a, const typename Cd:
 #pragma unroll
       for (int r = 0; r < R; ++r) Cd::mac(acc[r], v, xv[r]);
     }
+    // Slots to sum: the whole warp for a chunk, the V slots of a row otherwise.
+    const int span = kind == kSlicedChunk ? 32 : 1 << (a.llog2 + vwl);
     double d[R];
+    if constexpr (Cd::kPairReduce) {
+      // Double-float: sum the slots as (hi, lo) pairs on the FP32 pipe and
+      // convert once (each FP64 operation costs 64 FP32 issue slots here).
+      for (int off = 1 << a.llog2; off < span; off <<= 1)
 #pragma unroll
-    for (int r = 0; r < R; ++r) d[r] = Cd::out(acc[r]);
-    if (kind == kSlicedChunk) {
-      for (int off = 1 << a.llog2; off < 32; off <<= 1)
+        for (int r = 0; r < R; ++r) Cd::add_shfl(acc[r], off);
+#pragma unroll
+      for (int r = 0; r < R; ++r) d[r] = Cd::out(acc[r]);
+    } else {
+#pragma unroll
+      for (int r = 0; r < R; ++r) d[r] = Cd::out(acc[r]);
+      for (int off = 1 << a.llog2; off < span; off <<= 1)
 #pragma unroll
         for (int r = 0; r < R; ++r) d[r] += __shfl_xor_sync(kFull, d[r], off);
+    }
+    if (kind == kSlicedChunk) {
       if (slot == 0) store_y<R>(a.chunk_sum + ((size_t)row_base << a.klog2) + sub * R, d);
       __threadfence();
       __syncwarp();
@@ -219,10 +244,6 @@ __device__ __forceinline__ void run_tasks(const BatchArgs& a, const typename Cd:
         if (lane == 0) a.chunk_count[li] = 0;
       }
     } else {
-      const int vspan = 1 << (a.llog2 + vwl);  // lanes of one row: L * V
-      for (int off = 1 << a.llog2; off < vspan; off <<= 1)
-#pragma unroll
-        for (int r = 0; r < R; ++r) d[r] += __shfl_xor_sync(kFull, d[r], off);
       const int g = slot >> vwl;
       if ((slot & ((1 << vwl) - 1)) == 0 && g < nrows)
         store_y<R>(a.y + ((size_t)__ldg(a.rowid + row_base + g) << a.klog2) + sub * R, d);
