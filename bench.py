@@ -22,7 +22,9 @@ during the timed region), `rel_error` (against the compensated FP64 oracle),
 `legs` (per matrix — the headline matrix and, for R-MAT 2^24, the 256^3
 27-point stencil — the plain FP64 sliced kernel, its FP32 / BF16+row-scale /
 FP32 hi+lo forms and the learned and rule-based kernel selections: median ms
-over --leg-steps flushed calls, speed-up over plain FP64, row-wise error).
+over --leg-steps flushed calls, speed-up over plain FP64, row-wise error),
+`batch_legs` (the batched form on 512 uneven matrices, k = 1 and 32, FP64 /
+FP32 / DF32, autotuned, 5 graph-replayed steps each).
 
 `--workload batch512` measures the batched multi-right-hand-side form instead
 (512 uneven matrices, k = 1..32, one graph-replayed persistent launch per step).
@@ -405,6 +407,15 @@ def run_ours(args) -> None:
             legs["stencil256"] = form_legs(m2, x2, algorithmic_bytes(m2), flush, stream, args.leg_steps, args.warmup)
             m2.free()
         line["legs"] = legs
+        if args.workload == "rmat24" and not args.no_batch_leg:
+            from vnec_gb300 import generators as G
+
+            mats = G.batch_lognormal(512, seed=0)
+            blegs, _, _ = batch_legs(mats, [1, 32], [api.PREC_FP64, api.PREC_FP32, api.PREC_DF32], 5, args.warmup,
+                                     dev, flush, stream, ws)
+            line["batch_legs"] = {"workload": BATCH_DESC, "legs": blegs}
+            for m3 in mats:
+                m3.free()
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         secs, reps, sample = cpu_time_L(m, xv, warm=1, reps=40, budget_s=args.cpu_budget)
         cores, _, _ = reference_cores_and_parts()
@@ -428,6 +439,103 @@ FP64_PEAK_TFLOPS = 1.25  # nominal GB300 FP64 (non-tensor) rate
 
 def batch_bytes(nnz: int, n_rows: int, n_cols: int, n_mats: int, k: int, vb: int = 8) -> int:
     return nnz * (vb + 4) + (n_rows + n_mats) * 4 + (n_rows + n_cols) * k * 8
+
+
+def batch_legs(mats, ks, precs, steps: int, warmup: int, dev, flush, stream, ws: int = 1):
+    """Every (precision, k) of the batched form on `mats`: autotuned plan, graph
+    replays timed with CUDA events (L2 flushed before each), end-to-end host
+    calls and error on every 32nd matrix.  Returns (legs, launches, first leg)."""
+    import torch
+
+    from oracle import oracle as O
+    from vnec_gb300 import api
+
+    nnz = sum(m.nnz for m in mats)
+    n_rows = sum(m.n_rows for m in mats)
+    n_cols = sum(m.n_cols for m in mats)
+    peak, _ = measured_peaks()
+    legs = {}
+    gpu_launches = 0
+    first = None
+    rng = np.random.default_rng(1)
+    for prec in precs:
+        for k in ks:
+            t_plan = time.time()
+            plan = api.BatchPlan(mats, k, precision=prec, autotune=True)
+            t_plan = time.time() - t_plan
+            info = plan.info()
+            ro, co = plan.offsets()
+            xv = rng.uniform(-1, 1, n_cols * k)
+            x = torch.from_numpy(xv).to(dev)
+            y = torch.empty(n_rows * k, dtype=torch.float64, device=dev)
+            B = batch_bytes(nnz, n_rows, n_cols, len(mats), k, 4 if prec == api.PREC_FP32 else 8)
+            pname = {api.PREC_FP64: "fp64", api.PREC_FP32: "fp32", api.PREC_DF32: "df32"}[prec]
+            with torch.cuda.stream(stream):
+                for _ in range(warmup):
+                    flush.fill_(1)
+                    plan.mxv_device(x.data_ptr(), y.data_ptr(), stream.cuda_stream)
+            stream.synchronize()
+            starts = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+            ends = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+            if ws > 1:
+                torch.distributed.barrier()
+            torch.cuda.synchronize()
+            with torch.cuda.stream(stream):
+                for i in range(steps):
+                    flush.fill_(i)
+                    starts[i].record(stream)
+                    plan.mxv_device(x.data_ptr(), y.data_ptr(), stream.cuda_stream)
+                    ends[i].record(stream)
+            torch.cuda.synchronize()
+            ms = [a.elapsed_time(b) for a, b in zip(starts, ends)]
+            total = replica_max(float(np.sum(ms)), dev)
+            gpu_launches += steps * info.launches_per_call
+            value = replica_throughput(B, steps, ws, total)
+            # end to end: pinned host X / Y through SpB_mxv_host_ext
+            hx = torch.from_numpy(xv).pin_memory()
+            hy = torch.empty(n_rows * k, dtype=torch.float64).pin_memory()
+            plan.mxv_host(hx.numpy(), hy.numpy())
+            e2e_steps = max(1, steps // 4)
+            t0 = time.perf_counter()
+            for _ in range(e2e_steps):
+                plan.mxv_host(hx.numpy(), hy.numpy())
+            e2e_s = time.perf_counter() - t0
+            y_dev = y.cpu().numpy()
+            if not np.array_equal(hy.numpy(), y_dev):
+                raise RuntimeError("host-path and device-path batch results differ")
+            errs = []
+            for i in range(0, len(mats), max(1, len(mats) // 16)):
+                m = mats[i]
+                Yr, cond = O.spmm_neumaier(m, xv[co[i] * k:co[i + 1] * k].reshape(m.n_cols, k))
+                Yg = y_dev[ro[i] * k:ro[i + 1] * k].reshape(m.n_rows, k)
+                errs.append(O.rowwise_error(Yg, Yr, cond).ravel())
+            rel = np.concatenate(errs)
+            cand, tms, best = plan.tuning()
+            mean_ms = total / steps
+            leg = {"k": k, "precision": pname,
+                   "gbs": round(value, 2), "ms_per_step": round(mean_ms, 4),
+                   "hbm_frac": round(B / (mean_ms / 1e3) / 1e9 / peak, 4),
+                   "fp64_tflops": round(2 * nnz * k / (mean_ms / 1e3) / 1e12, 4),
+                   "e2e_gbs": round(B * e2e_steps / e2e_s / 1e9, 2),
+                   "h2d_bytes_per_step": n_cols * k * 8, "d2h_bytes_per_step": n_rows * k * 8,
+                   "algorithmic_bytes": B, "lanes": info.lanes, "long_row_len": info.long_row_len,
+                   "threads_per_block": info.threads_per_block, "tasks": info.num_tiles,
+                   "tuner": {"candidates": len(cand), "best_ms_on_sample": round(tms[best], 4) if cand else None,
+                             "worst_ms_on_sample": round(max(tms), 4) if cand else None,
+                             "chosen": list(cand[best]) if cand else None},
+                   "plan_build_s": round(t_plan, 2), "launches_per_call": info.launches_per_call,
+                   "rel_error": {"max": float(rel.max()), "median": float(np.median(rel))}}
+            legs[f"{pname}_k{k}"] = leg
+            if first is None:
+                first = (leg, B)
+            plan.free()
+            del x, y, hx, hy
+            torch.cuda.empty_cache()
+    for leg in legs.values():
+        base = legs.get(f"fp64_k{leg['k']}")
+        if base:
+            leg["speedup_vs_fp64"] = round(base["ms_per_step"] / leg["ms_per_step"], 3)
+    return legs, gpu_launches, first
 
 
 def run_batch(args) -> None:
@@ -459,85 +567,7 @@ def run_batch(args) -> None:
     peak, peak_src = measured_peaks()
     sampler = ClockSampler(dev.index)
     w0 = time.time()
-    legs = {}
-    gpu_launches = 0
-    first = None
-    rng = np.random.default_rng(1)
-    for prec in precs:
-        for k in ks:
-            t_plan = time.time()
-            plan = api.BatchPlan(mats, k, precision=prec, autotune=True)
-            t_plan = time.time() - t_plan
-            info = plan.info()
-            ro, co = plan.offsets()
-            xv = rng.uniform(-1, 1, n_cols * k)
-            x = torch.from_numpy(xv).to(dev)
-            y = torch.empty(n_rows * k, dtype=torch.float64, device=dev)
-            B = batch_bytes(nnz, n_rows, n_cols, len(mats), k, 4 if prec == api.PREC_FP32 else 8)
-            pname = {api.PREC_FP64: "fp64", api.PREC_FP32: "fp32", api.PREC_DF32: "df32"}[prec]
-            with torch.cuda.stream(stream):
-                for _ in range(args.warmup):
-                    flush.fill_(1)
-                    plan.mxv_device(x.data_ptr(), y.data_ptr(), stream.cuda_stream)
-            stream.synchronize()
-            starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.batch_steps)]
-            ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.batch_steps)]
-            if ws > 1:
-                torch.distributed.barrier()
-            torch.cuda.synchronize()
-            with torch.cuda.stream(stream):
-                for i in range(args.batch_steps):
-                    flush.fill_(i)
-                    starts[i].record(stream)
-                    plan.mxv_device(x.data_ptr(), y.data_ptr(), stream.cuda_stream)
-                    ends[i].record(stream)
-            torch.cuda.synchronize()
-            ms = [a.elapsed_time(b) for a, b in zip(starts, ends)]
-            total = replica_max(float(np.sum(ms)), dev)
-            gpu_launches += args.batch_steps * info.launches_per_call
-            value = replica_throughput(B, args.batch_steps, ws, total)
-            # end to end: pinned host X / Y through SpB_mxv_host_ext
-            hx = torch.from_numpy(xv).pin_memory()
-            hy = torch.empty(n_rows * k, dtype=torch.float64).pin_memory()
-            plan.mxv_host(hx.numpy(), hy.numpy())
-            e2e_steps = max(1, args.batch_steps // 4)
-            t0 = time.perf_counter()
-            for _ in range(e2e_steps):
-                plan.mxv_host(hx.numpy(), hy.numpy())
-            e2e_s = time.perf_counter() - t0
-            y_dev = y.cpu().numpy()
-            if not np.array_equal(hy.numpy(), y_dev):
-                raise RuntimeError("host-path and device-path batch results differ")
-            # accuracy on a sample of matrices against the compensated FP64 oracle
-            from oracle import oracle as O
-
-            errs = []
-            for i in range(0, len(mats), max(1, len(mats) // 16)):
-                m = mats[i]
-                Yr, cond = O.spmm_neumaier(m, xv[co[i] * k:co[i + 1] * k].reshape(m.n_cols, k))
-                Yg = y_dev[ro[i] * k:ro[i + 1] * k].reshape(m.n_rows, k)
-                errs.append(O.rowwise_error(Yg, Yr, cond).ravel())
-            rel = np.concatenate(errs)
-            cand, tms, best = plan.tuning()
-            mean_ms = total / args.batch_steps
-            leg = {"k": k, "precision": pname,
-                   "gbs": round(value, 2), "ms_per_step": round(mean_ms, 4),
-                   "hbm_frac": round(B / (mean_ms / 1e3) / 1e9 / peak, 4),
-                   "fp64_tflops": round(2 * nnz * k / (mean_ms / 1e3) / 1e12, 4),
-                   "e2e_gbs": round(B * e2e_steps / e2e_s / 1e9, 2),
-                   "h2d_bytes_per_step": n_cols * k * 8, "d2h_bytes_per_step": n_rows * k * 8,
-                   "algorithmic_bytes": B, "lanes": info.lanes, "long_row_len": info.long_row_len,
-                   "threads_per_block": info.threads_per_block, "tasks": info.num_tiles,
-                   "tuner": {"candidates": len(cand), "best_ms_on_sample": round(tms[best], 4) if cand else None,
-                             "worst_ms_on_sample": round(max(tms), 4) if cand else None},
-                   "plan_build_s": round(t_plan, 2), "launches_per_call": info.launches_per_call,
-                   "rel_error": {"max": float(rel.max()), "median": float(np.median(rel))}}
-            legs[f"{leg['precision']}_k{k}"] = leg
-            if first is None:
-                first = (leg, B)
-            plan.free()
-            del x, y, hx, hy
-            torch.cuda.empty_cache()
+    legs, gpu_launches, first = batch_legs(mats, ks, precs, args.batch_steps, args.warmup, dev, flush, stream, ws)
     w1 = time.time()
     clocks = sampler.stop(w0, w1)
     leg, B = first
@@ -607,7 +637,8 @@ def main() -> None:
     ap.add_argument("--batch-steps", type=int, default=10)
     ap.add_argument("--kernel", default="S", choices=["L", "S"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--no-legs", action="store_true", help="skip the precision-form / tuner legs")
+    ap.add_argument("--no-legs", action="store_true", help="skip the precision-form / tuner / batch legs")
+    ap.add_argument("--no-batch-leg", action="store_true", help="skip the batched-form legs of the default run")
     ap.add_argument("--leg-steps", type=int, default=100)
     ap.add_argument("--cpu-budget", type=float, default=20.0, help="seconds of CPU-baseline timing")
     args = ap.parse_args()
