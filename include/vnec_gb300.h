@@ -152,7 +152,9 @@ typedef struct {
   int transpose;         /* 1: the plan computes y := A^T x (the reference's SpB_TRAN0
                             descriptor, OpenSparseBLAS.h:62-72): x has n_rows entries,
                             y n_cols; any kernel, built on A's transpose */
-  int reserved[3];
+  int host_parts;        /* sliced FP64 plans: host-vector calls run in this many parts so
+                            that y copies overlap the SpMV (0: 8, 1: one part) */
+  int reserved[2];
 } SpB_VNEC_options_ext;
 
 /* Precision forms of the sliced kernel for an FP64 matrix (x and y stay

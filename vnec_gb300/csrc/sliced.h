@@ -44,6 +44,7 @@ struct SlicedMatrix {
   int hot = 0;
   const int32_t* hot_cols = nullptr;  // original column of each slot
   void* xhot = nullptr;               // FP64 kernel: hot x values
+  bool hot_ready = false;             // xhot already gathered for this call (later parts of a split call)
 };
 
 struct SlicedParams {
@@ -76,6 +77,12 @@ struct SlicedHostView {
   const int32_t* long_row;
   const int32_t* long_first;
   int vpe;
+  // Windows of window_rows rows in row order: tasks, long rows and entries of
+  // window w start at win_task[w], win_long[w], win_entry[w].
+  int64_t num_windows;
+  const int64_t* win_task;
+  const int64_t* win_long;
+  const int64_t* win_entry;
 };
 SlicedHostView sliced_view(const SlicedHost* h);
 
@@ -88,6 +95,9 @@ struct SlicedEpilogue {
 
 bool sliced_spmv(const SlicedMatrix& m, bool fp64, const void* x, void* y, cudaStream_t s,
                  cudaEvent_t* events = nullptr, const SlicedEpilogue* epi = nullptr);
+// Gathers the hot-column window's x values of a call (the first step of the
+// sliced kernel when hot_ready is false).
+bool sliced_gather_hot(const SlicedMatrix& m, bool fp64, const void* x, cudaStream_t s);
 // y[0..n) := alpha * y + beta * z + gamma (the unfused form of the epilogue).
 bool apply_epilogue(void* y, long long n, bool fp64, const SlicedEpilogue& e, cudaStream_t s);
 

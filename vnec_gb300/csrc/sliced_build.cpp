@@ -26,6 +26,7 @@ namespace vnec {
 struct SlicedHost {
   int64_t entries = 0, n_rowid = 0, num_long = 0, num_chunks = 0;
   int vpe = 1;
+  std::vector<int64_t> win_task, win_long, win_entry;  // per-window offsets (windows + 1)
   std::vector<SlicedTask> tasks;
   std::unique_ptr<unsigned char[]> val;
   std::unique_ptr<int32_t[]> col;
@@ -145,6 +146,9 @@ SlicedHost* sliced_build(int64_t n_rows, int64_t n_cols, const int64_t* rp, cons
   h->n_rowid = off_r[nwin];
   h->num_chunks = off_c[nwin];
   h->num_long = off_l[nwin];
+  h->win_task = off_t;
+  h->win_long = off_l;
+  h->win_entry = off_e;
   h->tasks.resize((size_t)off_t[nwin]);
   h->rowid.resize((size_t)off_r[nwin]);
   h->long_row.resize((size_t)off_l[nwin]);
@@ -232,6 +236,10 @@ SlicedHostView sliced_view(const SlicedHost* h) {
   v.long_row = h->long_row.data();
   v.long_first = h->long_first.data();
   v.vpe = h->vpe;
+  v.num_windows = (int64_t)h->win_task.size() - 1;
+  v.win_task = h->win_task.data();
+  v.win_long = h->win_long.data();
+  v.win_entry = h->win_entry.data();
   return v;
 }
 

@@ -304,7 +304,7 @@ bool launch_main(const SlicedMatrix& m, const void* x, void* y, cudaStream_t s,
     set_error("sliced: too many tasks for one launch");
     return false;
   }
-  if (HOT) {
+  if (HOT && !m.hot_ready) {
     gather_hot<V><<<(unsigned)((m.hot + 255) / 256), 256, 0, s>>>(static_cast<const V*>(x), m.hot_cols, m.hot,
                                                                   static_cast<V*>(m.xhot));
     if (!VNEC_CUDA(cudaGetLastError())) return false;
@@ -400,6 +400,16 @@ bool sliced_guard_f64(const SlicedMatrix& m, const double* x, double* y, const i
 bool sliced_spmv(const SlicedMatrix& m, bool fp64, const void* x, void* y, cudaStream_t s, cudaEvent_t* ev,
                  const SlicedEpilogue* epi) {
   return fp64 ? launch<double>(m, x, y, s, ev, epi) : launch<float>(m, x, y, s, ev, epi);
+}
+
+bool sliced_gather_hot(const SlicedMatrix& m, bool fp64, const void* x, cudaStream_t s) {
+  if (m.hot <= 0) return true;
+  const unsigned g = (unsigned)((m.hot + 255) / 256);
+  if (fp64)
+    gather_hot<double><<<g, 256, 0, s>>>(static_cast<const double*>(x), m.hot_cols, m.hot, static_cast<double*>(m.xhot));
+  else
+    gather_hot<float><<<g, 256, 0, s>>>(static_cast<const float*>(x), m.hot_cols, m.hot, static_cast<float*>(m.xhot));
+  return VNEC_CUDA(cudaGetLastError());
 }
 
 bool apply_epilogue(void* y, long long n, bool fp64, const SlicedEpilogue& e, cudaStream_t s) {

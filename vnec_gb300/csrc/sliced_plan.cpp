@@ -20,7 +20,86 @@ struct SlicedPlan final : Plan {
   std::vector<int32_t> hot_host;  // hot-column window: original column of each slot
   SlicedParams prm;
   int64_t blocks = 0;  // dense-block plans: number of blocks of 4
+  // Host-vector calls are split into parts (consecutive row windows) so that
+  // the copy of one part's y rows to the host overlaps the next part's SpMV.
+  struct Part {
+    int64_t t0, t1, l0, l1, r0, r1;  // task, long-row and row ranges
+  };
+  std::vector<Part> parts;
+  // Each part runs on its own stream, with stream priorities falling from the
+  // first part to the last: all parts are launched together once x is on the
+  // device, the block scheduler serves earlier parts first, so parts finish in
+  // order while later parts fill the SMs that earlier parts' tails leave idle;
+  // copy_stream carries each part's y copy as soon as that part is done.
+  cudaStream_t copy_stream = nullptr;
+  std::vector<cudaStream_t> part_streams;
+  cudaEvent_t x_ready = nullptr;
+  std::vector<cudaEvent_t> part_done;
   explicit SlicedPlan(PlanKind k) : Plan(k) {}
+  ~SlicedPlan() override {
+    for (cudaEvent_t e : part_done)
+      if (e) cudaEventDestroy(e);
+    if (x_ready) cudaEventDestroy(x_ready);
+    if (copy_stream) cudaStreamDestroy(copy_stream);
+    for (cudaStream_t q : part_streams)
+      if (q) cudaStreamDestroy(q);
+  }
+  bool ensure_part_streams() {
+    if (part_streams.size() == parts.size()) return true;
+    int least = 0, greatest = 0;
+    if (!VNEC_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest))) return false;
+    const int levels = least - greatest + 1;  // greatest is the numerically lowest
+    for (size_t i = part_streams.size(); i < parts.size(); ++i) {
+      const int prio = greatest + (int)((int64_t)i * levels / (int64_t)parts.size());
+      cudaStream_t q = nullptr;
+      if (!VNEC_CUDA(cudaStreamCreateWithPriority(&q, cudaStreamNonBlocking, std::min(prio, least)))) return false;
+      part_streams.push_back(q);
+    }
+    return true;
+  }
+  bool run_host(const void* h_x, void* h_y) override {
+    if (mx.precision != kPrecFP64 || m.vpe != 1 || parts.size() < 2 || profiling) return Plan::run_host(h_x, h_y);
+    std::lock_guard<std::mutex> g(host_mu);
+    const size_t vb = type == SpB_FP64 ? 8 : 4;
+    if (!own_stream && !VNEC_CUDA(cudaStreamCreateWithFlags(&own_stream, cudaStreamNonBlocking))) return false;
+    if (!copy_stream && !VNEC_CUDA(cudaStreamCreateWithFlags(&copy_stream, cudaStreamNonBlocking))) return false;
+    if (!ensure_part_streams()) return false;
+    if (!x_ready && !VNEC_CUDA(cudaEventCreateWithFlags(&x_ready, cudaEventDisableTiming))) return false;
+    while (part_done.size() < parts.size()) {
+      cudaEvent_t e = nullptr;
+      if (!VNEC_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming))) return false;
+      part_done.push_back(e);
+    }
+    if (!dx.ptr && !dx.alloc(vb * (size_t)std::max<int64_t>(n_cols, 1))) return false;
+    if (!dy.ptr && !dy.alloc(vb * (size_t)std::max<int64_t>(n_rows, 1))) return false;
+    if (n_cols > 0 && !VNEC_CUDA(cudaMemcpyAsync(dx.ptr, h_x, vb * n_cols, cudaMemcpyHostToDevice, own_stream)))
+      return false;
+    if (!sliced_gather_hot(m, type == SpB_FP64, dx.ptr, own_stream) || !VNEC_CUDA(cudaEventRecord(x_ready, own_stream)))
+      return false;
+    for (size_t i = 0; i < parts.size(); ++i) {
+      const Part& q = parts[i];
+      cudaStream_t cs = part_streams[i];
+      if (!VNEC_CUDA(cudaStreamWaitEvent(cs, x_ready, 0))) return false;
+      SlicedMatrix mp = m;
+      mp.tasks = m.tasks + q.t0;
+      mp.num_tasks = q.t1 - q.t0;
+      mp.long_row = m.long_row + q.l0;
+      mp.long_first = m.long_first + q.l0;
+      mp.num_long = q.l1 - q.l0;
+      mp.hot_ready = true;  // gathered above
+      if (!sliced_spmv(mp, type == SpB_FP64, dx.ptr, dy.ptr, cs) || !VNEC_CUDA(cudaEventRecord(part_done[i], cs)) ||
+          !VNEC_CUDA(cudaStreamWaitEvent(copy_stream, part_done[i], 0)))
+        return false;
+      if (q.r1 > q.r0 &&
+          !VNEC_CUDA(cudaMemcpyAsync(static_cast<char*>(h_y) + vb * q.r0, static_cast<char*>(dy.ptr) + vb * q.r0,
+                                     vb * (q.r1 - q.r0), cudaMemcpyDeviceToHost, copy_stream)))
+        return false;
+    }
+    if (!VNEC_CUDA(cudaStreamSynchronize(copy_stream))) return false;
+    for (cudaStream_t q : part_streams)
+      if (!VNEC_CUDA(cudaStreamSynchronize(q))) return false;
+    return device_status(own_stream);
+  }
   bool run(const void* d_x, void* d_y, cudaStream_t s) override {
     if (profiling && !ensure_events()) return false;
     if (mx.precision != kPrecFP64)
@@ -144,7 +223,7 @@ uint16_t to_bf16(double v) {
 // Uploads a built host layout into a plan.  `row_exp` (BF16 form): the
 // power-of-two exponent each row was scaled by.
 std::unique_ptr<Plan> upload(std::unique_ptr<SlicedPlan> p, SlicedHost* h, int vb, const SpB_VNEC_options_ext* opts,
-                             const std::vector<signed char>* row_exp = nullptr) {
+                             const std::vector<signed char>* row_exp = nullptr, bool keep_mask = false) {
   std::unique_ptr<SlicedHost, void (*)(SlicedHost*)> guard(h, sliced_free);
   SlicedHostView hv = sliced_view(h);
   const size_t pad = 64;
@@ -229,6 +308,22 @@ std::unique_ptr<Plan> upload(std::unique_ptr<SlicedPlan> p, SlicedHost* h, int v
   m.cache_hints = (opts && opts->cache_hints >= 2 && opts->cache_hints <= 4) ? opts->cache_hints - 1 : 0;
   const int ipt = opts ? opts->items_per_thread : 0;
   m.unroll = (ipt == 4 || ipt == 8 || ipt == 12 || ipt == 16) ? ipt : 12;
+  // Parts for host-vector calls: about 8 groups of whole windows with equal
+  // entries (only plans that compute every row: no keep mask).
+  const int kParts = (opts && opts->host_parts > 0) ? std::min(opts->host_parts, 1024) : 8;
+  if (hv.num_windows > 1 && !keep_mask && kParts > 1) {
+    const int64_t W = p->prm.window_rows;
+    int64_t w0 = 0;
+    for (int i = 1; i <= kParts && w0 < hv.num_windows; ++i) {
+      const int64_t target = hv.entries * i / kParts;
+      int64_t w1 = w0 + 1;
+      while (w1 < hv.num_windows && hv.win_entry[w1] < target) ++w1;
+      if (i == kParts) w1 = hv.num_windows;
+      p->parts.push_back(SlicedPlan::Part{hv.win_task[w0], hv.win_task[w1], hv.win_long[w0], hv.win_long[w1],
+                                          w0 * W, std::min<int64_t>(p->n_rows, w1 * W)});
+      w0 = w1;
+    }
+  }
   return p;
 }
 
@@ -313,7 +408,7 @@ std::unique_ptr<Plan> build_sliced(const CsrView& v, const SpB_VNEC_options_ext*
     set_error("sliced format: more than 2^31 entries or row slots");
     return nullptr;
   }
-  return upload(std::move(p), h, vb, opts, prec == kPrecBF16 ? &row_exp : nullptr);
+  return upload(std::move(p), h, vb, opts, prec == kPrecBF16 ? &row_exp : nullptr, keep != nullptr);
 }
 
 // Dense-block format (VNEC-D counterpart, spmv_vnec_D_for_mxv.c:242-398):
@@ -372,7 +467,7 @@ std::unique_ptr<Plan> build_dense(const CsrView& v, const SpB_VNEC_options_ext* 
     set_error("dense-block format: more than 2^31 blocks or row slots");
     return nullptr;
   }
-  return upload(std::move(p), h, vb, opts);
+  return upload(std::move(p), h, vb, opts, nullptr, keep != nullptr);
 }
 
 namespace {
