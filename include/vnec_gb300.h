@@ -348,7 +348,9 @@ typedef struct {
   int window_rows;     /* rows sorted by length within windows of this size (0: 65536) */
   int max_steps;       /* a row group spreads over enough slots to take at most this many steps (0: 32) */
   int unroll;          /* load steps in flight per lane: 1 normal, 2 doubled; 0: tuned or normal */
-  int reserved[6];
+  int host_parts;      /* host-vector calls run in this many parts so that X and Y copies overlap the
+                          compute (0: 8, 1: one part) */
+  int reserved[5];
 } SpB_VNEC_batch_options_ext;
 
 /* Plan from host CSR arrays per matrix: int64 row offsets (n_rows[m] + 1),

@@ -154,6 +154,37 @@ def test_batch_df32_rejects_out_of_range_values(built, batch):
         api.BatchPlan([batch[0], bad], 4, precision=api.PREC_DF32)
 
 
+@pytest.mark.parametrize("precision", [0, 1, 3], ids=["fp64", "fp32", "df32"])
+def test_batch_host_calls_in_parts(built, precision):
+    """Host-vector calls copy X in, compute and copy Y out part by part (groups
+    of row windows, each with the X rows of its matrices): bit-identical to the
+    device-pointer call for any number of parts, including windows that split a
+    matrix and matrices without rows."""
+    import torch
+
+    from vnec_gb300 import api
+
+    mats = small_batch(seed=9, n=24)
+    k = 4
+    outs = []
+    for parts in (1, 3, 8, 64):
+        p = api.BatchPlan(mats, k, precision=precision, window_rows=500, host_parts=parts, long_row_len=128)
+        try:
+            ro, co = p.offsets()
+            X = _x(p, k, seed=4)
+            Y = p.mxv_host(X)
+            x = torch.from_numpy(X).cuda()
+            y = torch.full((int(ro[-1]) * k,), float("nan"), dtype=torch.float64, device="cuda")
+            p.mxv_device(x.data_ptr(), y.data_ptr())
+            torch.cuda.synchronize()
+            assert y.cpu().numpy().tobytes() == Y.reshape(-1).tobytes(), parts
+            outs.append(Y)
+        finally:
+            p.free()
+    Yref, cond = oracle_batch(mats, X, k, co, ro)
+    check(outs[-1], Yref, cond, TOL[precision])
+
+
 def test_batch_graph_pointer_changes(built, batch):
     """The captured graph follows the (x, y) pair of each call."""
     import torch

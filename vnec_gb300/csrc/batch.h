@@ -65,6 +65,9 @@ struct BatchHostView {
   const int32_t* long_first;
   const int32_t* chunk_long;
   int lanes;
+  int64_t num_windows;      // windows of window_rows global rows
+  const int64_t* win_task;  // first task of each window (num_windows + 1)
+  const int64_t* win_entry; // first entry of each window (num_windows + 1)
 };
 BatchHostView batch_view(const BatchHost* h);
 
@@ -76,6 +79,11 @@ int batch_grid(int precision, int rhs_per_lane, int warps_per_block, bool deep);
 // rounds X into xbuf).  Long rows are finished inside the kernel by the last
 // of their chunks to arrive.
 bool batch_spmm(const BatchMatrix& m, const double* X, double* Y, cudaStream_t s);
+// One part of a call: converts X columns [c0, c1) (FP32 / DF32 forms; `first`
+// clears the DF32 range flag) and runs tasks [t0, t1).  Parts of whole windows
+// write disjoint Y rows; a long row's chunks never straddle two windows.
+bool batch_spmm_range(const BatchMatrix& m, const double* X, double* Y, cudaStream_t s, int64_t t0, int64_t t1,
+                      int64_t c0, int64_t c1, bool first);
 inline int batch_launches(const BatchMatrix& m) { return m.precision == kPrecFP64 ? 1 : 2; }
 
 }  // namespace vnec

@@ -25,6 +25,7 @@ namespace vnec {
 struct BatchHost {
   int64_t n_rows = 0, n_cols = 0, nnz = 0, entries = 0, n_rowid = 0, num_long = 0, num_chunks = 0;
   int lanes = 1;
+  std::vector<int64_t> win_task, win_entry;
   std::vector<SlicedTask> tasks;
   std::unique_ptr<double[]> val;
   std::unique_ptr<int32_t[]> col;
@@ -170,6 +171,8 @@ BatchHost* batch_build(int n, const int64_t* n_rows, const int64_t* n_cols, cons
   h->n_rowid = off_r[nwin];
   h->num_chunks = off_c[nwin];
   h->num_long = off_l[nwin];
+  h->win_task = off_t;
+  h->win_entry = off_e;
   h->tasks.resize((size_t)off_t[nwin]);
   h->rowid.resize((size_t)off_r[nwin]);
   h->long_row.resize((size_t)off_l[nwin]);
@@ -287,6 +290,9 @@ BatchHostView batch_view(const BatchHost* h) {
   v.long_first = h->long_first.data();
   v.chunk_long = h->chunk_long.data();
   v.lanes = h->lanes;
+  v.num_windows = (int64_t)h->win_task.size() - 1;
+  v.win_task = h->win_task.data();
+  v.win_entry = h->win_entry.data();
   return v;
 }
 

@@ -306,25 +306,30 @@ int batch_grid(int precision, int rhs_per_lane, int warps_per_block, bool deep) 
 }
 
 bool batch_spmm(const BatchMatrix& m, const double* X, double* Y, cudaStream_t s) {
+  return batch_spmm_range(m, X, Y, s, 0, m.num_tasks, 0, m.n_cols, true);
+}
+
+bool batch_spmm_range(const BatchMatrix& m, const double* X, double* Y, cudaStream_t s, int64_t t0, int64_t t1,
+                      int64_t c0, int64_t c1, bool first) {
   if (!batch_supported(m.k, m.lanes)) {
     set_error("batch: unsupported k / lanes");
     return false;
   }
   const int R = m.k / m.lanes;
   const void* xin = X;
-  const long long nx = (long long)m.n_cols * m.k;
+  const long long off = (long long)c0 * m.k, nx = (long long)(c1 - c0) * m.k;
   if (m.precision == kPrecFP32) {
-    if (nx > 0 && !round_to_f32(X, static_cast<float*>(m.xbuf), nx, s)) return false;
+    if (nx > 0 && !round_to_f32(X + off, static_cast<float*>(m.xbuf) + off, nx, s)) return false;
     xin = m.xbuf;
   } else if (m.precision == kPrecDF32) {
-    if (!VNEC_CUDA(cudaMemsetAsync(m.flag, 0, sizeof(int), s))) return false;
-    if (nx > 0 && !split_to_df32(X, static_cast<float2*>(m.xbuf), nx, m.flag, s)) return false;
+    if (first && !VNEC_CUDA(cudaMemsetAsync(m.flag, 0, sizeof(int), s))) return false;
+    if (nx > 0 && !split_to_df32(X + off, static_cast<float2*>(m.xbuf) + off, nx, m.flag, s)) return false;
     xin = m.xbuf;
   }
-  if (m.num_tasks == 0) return true;
+  if (t1 <= t0) return true;
   BatchArgs a;
-  a.tasks = reinterpret_cast<const int4*>(m.tasks);
-  a.num_tasks = m.num_tasks;
+  a.tasks = reinterpret_cast<const int4*>(m.tasks) + t0;
+  a.num_tasks = t1 - t0;
   a.val = m.val;
   a.col = m.col;
   a.rowid = m.rowid;
@@ -340,7 +345,7 @@ bool batch_spmm(const BatchMatrix& m, const double* X, double* Y, cudaStream_t s
   a.klog2 = log2i(m.k);
   a.llog2 = log2i(m.lanes);
   void* fn = pick_kernel(m.precision, R, m.deep);
-  const int grid = (int)std::min<long long>(m.grid, std::max<long long>(1, (m.num_tasks + 7) / 8));
+  const int grid = (int)std::min<long long>(m.grid, std::max<long long>(1, (a.num_tasks + 7) / 8));
   void* args[] = {&a};
   return VNEC_CUDA(cudaLaunchKernel(fn, dim3((unsigned)grid), dim3((unsigned)(m.warps_per_block * 32)), args, 0, s));
 }

@@ -394,11 +394,67 @@ struct BatchPlan final : Plan {
   const void* gx = nullptr;
   void* gy = nullptr;
 
+  // Host-vector calls run in parts of whole row windows.  The concatenation
+  // is block-diagonal, so the rows of a part read only the X rows of the
+  // matrices they belong to: part i's X rows are copied in on in_stream, its
+  // tasks run on own_stream once they have arrived, and its Y rows are copied
+  // out on out_stream — copies in both directions overlap the compute.
+  struct Part {
+    int64_t t0, t1, r0, r1, c0, c1;  // tasks, Y rows, X rows (new in this part)
+  };
+  std::vector<Part> parts;
+  cudaStream_t in_stream = nullptr, out_stream = nullptr;
+  std::vector<cudaEvent_t> x_in, done;
+
   BatchPlan() : Plan(PlanKind::kBatch) {}
   ~BatchPlan() override {
     if (exec) cudaGraphExecDestroy(exec);
     if (graph) cudaGraphDestroy(graph);
     if (cap) cudaStreamDestroy(cap);
+    for (cudaEvent_t e : x_in)
+      if (e) cudaEventDestroy(e);
+    for (cudaEvent_t e : done)
+      if (e) cudaEventDestroy(e);
+    if (in_stream) cudaStreamDestroy(in_stream);
+    if (out_stream) cudaStreamDestroy(out_stream);
+  }
+
+  bool run_host(const void* h_x, void* h_y) override {
+    if (parts.size() < 2 || profiling) return Plan::run_host(h_x, h_y);
+    std::lock_guard<std::mutex> g(host_mu);
+    const size_t row_bytes = sizeof(double) * (size_t)rhs;
+    if (!own_stream && !VNEC_CUDA(cudaStreamCreateWithFlags(&own_stream, cudaStreamNonBlocking))) return false;
+    if (!in_stream && !VNEC_CUDA(cudaStreamCreateWithFlags(&in_stream, cudaStreamNonBlocking))) return false;
+    if (!out_stream && !VNEC_CUDA(cudaStreamCreateWithFlags(&out_stream, cudaStreamNonBlocking))) return false;
+    while (x_in.size() < parts.size()) {
+      cudaEvent_t a = nullptr, b = nullptr;
+      if (!VNEC_CUDA(cudaEventCreateWithFlags(&a, cudaEventDisableTiming)) ||
+          !VNEC_CUDA(cudaEventCreateWithFlags(&b, cudaEventDisableTiming)))
+        return false;
+      x_in.push_back(a);
+      done.push_back(b);
+    }
+    if (!dx.ptr && !dx.alloc(row_bytes * (size_t)std::max<int64_t>(n_cols, 1))) return false;
+    if (!dy.ptr && !dy.alloc(row_bytes * (size_t)std::max<int64_t>(n_rows, 1))) return false;
+    for (size_t i = 0; i < parts.size(); ++i) {
+      const Part& q = parts[i];
+      if (q.c1 > q.c0 &&
+          !VNEC_CUDA(cudaMemcpyAsync(static_cast<char*>(dx.ptr) + row_bytes * q.c0,
+                                     static_cast<const char*>(h_x) + row_bytes * q.c0, row_bytes * (q.c1 - q.c0),
+                                     cudaMemcpyHostToDevice, in_stream)))
+        return false;
+      if (!VNEC_CUDA(cudaEventRecord(x_in[i], in_stream)) || !VNEC_CUDA(cudaStreamWaitEvent(own_stream, x_in[i], 0)) ||
+          !batch_spmm_range(d.m, dx.as<double>(), dy.as<double>(), own_stream, q.t0, q.t1, q.c0, q.c1, i == 0) ||
+          !VNEC_CUDA(cudaEventRecord(done[i], own_stream)) || !VNEC_CUDA(cudaStreamWaitEvent(out_stream, done[i], 0)))
+        return false;
+      if (q.r1 > q.r0 &&
+          !VNEC_CUDA(cudaMemcpyAsync(static_cast<char*>(h_y) + row_bytes * q.r0,
+                                     static_cast<char*>(dy.ptr) + row_bytes * q.r0, row_bytes * (q.r1 - q.r0),
+                                     cudaMemcpyDeviceToHost, out_stream)))
+        return false;
+    }
+    return VNEC_CUDA(cudaStreamSynchronize(out_stream)) && VNEC_CUDA(cudaStreamSynchronize(in_stream)) &&
+           device_status(own_stream);
   }
 
   bool capture(const void* d_x, void* d_y) {
@@ -470,6 +526,35 @@ struct BatchPlan final : Plan {
     info->long_row_len = prm.long_len;
   }
 };
+
+// Host-call parts: about `n_parts` groups of whole windows with equal
+// entries; part i copies in the X rows of the matrices its rows belong to that
+// earlier parts did not (the last part takes every remaining X row).
+void plan_parts(BatchPlan* p, const BatchHostView& hv, int n_parts) {
+  p->parts.clear();
+  if (hv.num_windows < 2 || n_parts < 2) return;
+  const int64_t W = p->prm.window_rows;
+  const int n = (int)p->row_off.size() - 1;
+  int64_t w0 = 0, c_done = 0;
+  for (int i = 1; i <= n_parts && w0 < hv.num_windows; ++i) {
+    const int64_t target = hv.win_entry[hv.num_windows] * i / n_parts;
+    int64_t w1 = w0 + 1;
+    while (w1 < hv.num_windows && hv.win_entry[w1] < target) ++w1;
+    if (i == n_parts) w1 = hv.num_windows;
+    const int64_t r0 = w0 * W, r1 = std::min<int64_t>(p->n_rows, w1 * W);
+    int64_t c1 = c_done;
+    if (w1 == hv.num_windows) {
+      c1 = p->n_cols;
+    } else if (r1 > r0) {
+      // matrix of the part's last row: the last m with row_off[m] <= r1 - 1
+      const int m = (int)(std::upper_bound(p->row_off.begin(), p->row_off.end(), r1 - 1) - p->row_off.begin()) - 1;
+      c1 = std::max(c_done, p->col_off[(size_t)std::min(m + 1, n)]);
+    }
+    p->parts.push_back(BatchPlan::Part{hv.win_task[w0], hv.win_task[w1], r0, r1, c_done, c1});
+    c_done = c1;
+    w0 = w1;
+  }
+}
 
 }  // namespace
 
@@ -586,6 +671,7 @@ std::unique_ptr<Plan> build_batch(int n, const CsrView* mats, int k, const SpB_V
     return nullptr;
   }
   const bool ok = upload_batch(h, k, o.precision, choice.wpb, choice.deep != 0, &p->d);
+  if (ok) plan_parts(p.get(), batch_view(h), o.host_parts > 0 ? o.host_parts : 8);
   batch_free(h);
   if (!ok) return nullptr;
   return p;
