@@ -258,6 +258,23 @@ def run_reference(args) -> None:
     ws, rank, _ = dist_env()
     if rank != 0:
         return
+    if args.workload == "batch512":
+        from vnec_gb300 import generators as G
+
+        mats = G.batch_lognormal(args.batch_mats, seed=0)
+        k = int(args.rhs.split(",")[-1])
+        cb = batch_cpu_baseline(mats, k, args.cpu_budget)
+        B = batch_bytes(sum(m.nnz for m in mats), sum(m.n_rows for m in mats), sum(m.n_cols for m in mats),
+                        len(mats), k)
+        line = {"impl": "reference", "metric": METRIC, "value": cb["value"], "unit": "GB/s", "n_gpus": ws,
+                "steps": 1, "warmup": 1, "ms_per_step": round(B / (cb["value"] * 1e9) * 1e3, 3),
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                "data": "synthetic (seeded generator)",
+                "config": {"workload": f"batch512_lognormal_fp64_k{k}", "desc": BATCH_DESC, "algorithmic_bytes": B},
+                "cpu_baseline": cb,
+                "e2e": {"value": cb["value"], "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line), flush=True)
+        return
     m, x, desc = workload(args.workload)
     B = algorithmic_bytes(m)
     cores, nparts, arch = reference_cores_and_parts()
@@ -618,7 +635,7 @@ def batch_cpu_baseline(mats, k: int, budget_s: float) -> dict:
         if time.time() - t_start > budget_s:
             break
     return {"value": round(B_total / t_total / 1e9, 3), "unit": "GB/s", "cores": cores, "kind": "port",
-            "sample": f"{len(pick)} of {len(mats)} matrices (every 16th in nnz order), SpMV_VNEC_L_FP64 restated "
+            "sample": f"{len(pick)} of {len(mats)} matrices (evenly spaced in nnz order), SpMV_VNEC_L_FP64 restated "
                       f"(oracle port) per matrix, 1 warm-up + 3 timed calls, x {k} right-hand sides; "
                       f"{nparts} OpenMP threads on {cores} {arch} cores"}
 
