@@ -228,9 +228,10 @@ def form_legs(m, xv, B: int, flush, stream, steps: int, warmup: int) -> dict:
     x = torch.from_numpy(xv).to(flush.device)
     y = torch.empty(m.n_rows, dtype=torch.float64, device=flush.device)
     legs = {}
-    forms = [("fp64", dict(kernel=api.KERNEL_S)), ("fp32", dict(kernel=api.KERNEL_S, precision=api.PREC_FP32)),
-             ("bf16_rowscale", dict(kernel=api.KERNEL_S, precision=api.PREC_BF16)),
-             ("df32_hilo", dict(kernel=api.KERNEL_S, precision=api.PREC_DF32)),
+    S = dict(kernel=api.KERNEL_S, items_per_thread=-1)  # unroll timed on the matrix at plan build
+    forms = [("fp64", S), ("fp32", dict(S, precision=api.PREC_FP32)),
+             ("bf16_rowscale", dict(S, precision=api.PREC_BF16)),
+             ("df32_hilo", dict(S, precision=api.PREC_DF32)),
              ("learned", dict(kernel=api.KERNEL_LEARNED)), ("rule", dict(kernel=api.KERNEL_RULE))]
     base = None
     for name, kw in forms:
@@ -240,6 +241,7 @@ def form_legs(m, xv, B: int, flush, stream, steps: int, warmup: int) -> dict:
         ms = float(np.median(time_plan_device(plan, x, y, flush, stream, steps, warmup)))
         rel = O.rowwise_error(y.cpu().numpy(), y_ref, cond)
         leg = {"ms": round(ms, 5), "gbs_plain_bytes": round(B / ms / 1e6, 1), "launches": plan.info().launches_per_call,
+               "unroll": plan.info().items_per_thread,
                "max_rel_error": float(rel.max()), "median_rel_error": float(np.median(rel)),
                "plan_build_s": round(build_s, 2)}
         if name in ("learned", "rule"):
@@ -315,7 +317,8 @@ def run_ours(args) -> None:
     B = algorithmic_bytes(m)
     t_plan = time.time()
     kernel = {"L": api.KERNEL_L, "S": api.KERNEL_S}[args.kernel]
-    plan = api.Plan(m, kernel=kernel)
+    # Sliced plans time their unroll (4/8/12/16 loads in flight) on the matrix at build.
+    plan = api.Plan(m, kernel=kernel, items_per_thread=-1 if args.kernel == "S" else 0)
     t_plan = time.time() - t_plan
     info = plan.info()
     stream = torch.cuda.Stream(device=dev)

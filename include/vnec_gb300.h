@@ -136,7 +136,8 @@ typedef enum {
 typedef struct {
   int kernel;            /* SpB_VNEC_kernel_ext */
   int threads_per_block; /* 0: default */
-  int items_per_thread;  /* 0: default */
+  int items_per_thread;  /* 0: default; sliced plans: load steps in flight 4/8/12/16,
+                            -1: timed on the matrix at plan build */
   int pipeline_stages;   /* merge-path: 0 default (2), 1 unpipelined kernel, 2-3 stages */
   int arithmetic;        /* SpB_VNEC_arith_ext (FP64 values) */
   int window_rows;       /* sliced: rows sorted within windows of this size (0: 65536) */

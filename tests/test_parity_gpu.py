@@ -301,7 +301,7 @@ def test_golden_sliced_dropin(built, case, fp64):
         check_f32(y.values, m, g["x"])
 
 
-SLICED_PARAMS = [dict(), dict(window_rows=1000), dict(long_row_len=64), dict(max_steps=4),
+SLICED_PARAMS = [dict(), dict(window_rows=1000), dict(long_row_len=64), dict(max_steps=4), dict(items_per_thread=-1),
                  dict(window_rows=777, long_row_len=96, max_steps=8), dict(long_row_len=32, max_steps=1)]
 
 
@@ -615,8 +615,8 @@ def test_precision_forms_error_bounds(built, prec):
     for m in (G.rmat(16, 16 << 16, seed=7), G.lognormal(20000, sigma=2.5, cap=4096, seed=8),
               G.stencil27(20, seed=9)):
         xv = G.vector(m.n_cols, seed=9)
-        p = api.Plan(m, kernel=api.KERNEL_S, precision=prec)
-        assert p.info().precision == prec
+        p = api.Plan(m, kernel=api.KERNEL_S, precision=prec, items_per_thread=-1)
+        assert p.info().precision == prec and p.info().items_per_thread in (4, 8, 12, 16)
         y = p.mxv_host(xv)
         check_f64(y, m, xv, tol=PREC_TOL[prec])
         assert p.mxv_host(xv).tobytes() == y.tobytes()

@@ -44,6 +44,42 @@ struct SlicedPlan final : Plan {
     for (cudaStream_t q : part_streams)
       if (q) cudaStreamDestroy(q);
   }
+  // Picks the unroll (4, 8, 12 or 16 load steps in flight) by timing each on
+  // this matrix: median of 3 calls after one warm-up, x filled with a constant.
+  bool tune_unroll() {
+    const size_t vb = type == SpB_FP64 ? 8 : 4;
+    DeviceBuffer tx, ty;
+    cudaStream_t s = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    bool ok = tx.alloc(vb * (size_t)std::max<int64_t>(n_cols, 1)) && ty.alloc(vb * (size_t)std::max<int64_t>(n_rows, 1)) &&
+              VNEC_CUDA(cudaMemset(tx.ptr, 0x3f, tx.bytes)) &&
+              VNEC_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking)) && VNEC_CUDA(cudaEventCreate(&e0)) &&
+              VNEC_CUDA(cudaEventCreate(&e1));
+    float best = 0.f;
+    int best_u = 12;
+    for (int u : {4, 8, 12, 16}) {
+      if (!ok) break;
+      m.unroll = u;
+      std::vector<float> t;
+      for (int rep = 0; rep < 4 && ok; ++rep) {
+        ok = VNEC_CUDA(cudaEventRecord(e0, s)) && run(tx.ptr, ty.ptr, s) && VNEC_CUDA(cudaEventRecord(e1, s)) &&
+             VNEC_CUDA(cudaEventSynchronize(e1));
+        float ms = 0.f;
+        if (ok && rep > 0 && VNEC_CUDA(cudaEventElapsedTime(&ms, e0, e1))) t.push_back(ms);
+      }
+      if (!ok) break;
+      std::sort(t.begin(), t.end());
+      if (best == 0.f || t[1] < best) {
+        best = t[1];
+        best_u = u;
+      }
+    }
+    m.unroll = best_u;
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    if (s) cudaStreamDestroy(s);
+    return ok;
+  }
   bool ensure_part_streams() {
     if (part_streams.size() == parts.size()) return true;
     int least = 0, greatest = 0;
@@ -308,6 +344,7 @@ std::unique_ptr<Plan> upload(std::unique_ptr<SlicedPlan> p, SlicedHost* h, int v
   m.cache_hints = (opts && opts->cache_hints >= 2 && opts->cache_hints <= 4) ? opts->cache_hints - 1 : 0;
   const int ipt = opts ? opts->items_per_thread : 0;
   m.unroll = (ipt == 4 || ipt == 8 || ipt == 12 || ipt == 16) ? ipt : 12;
+  if (ipt == -1 && m.vpe == 1 && !p->tune_unroll()) return nullptr;
   // Parts for host-vector calls: about 8 groups of whole windows with equal
   // entries (only plans that compute every row: no keep mask).
   const int kParts = (opts && opts->host_parts > 0) ? std::min(opts->host_parts, 1024) : 8;
