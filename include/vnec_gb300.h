@@ -155,7 +155,10 @@ typedef struct {
                             y n_cols; any kernel, built on A's transpose */
   int host_parts;        /* sliced FP64 plans: host-vector calls run in this many parts so
                             that y copies overlap the SpMV (0: 8, 1: one part) */
-  int reserved[2];
+  int column_deltas;     /* sliced: store the columns of one-row-per-lane groups as 16-bit
+                            deltas where the gaps allow (0: on unless a hot-column window
+                            is used, -1: off) */
+  int reserved[1];
 } SpB_VNEC_options_ext;
 
 /* Precision forms of the sliced kernel for an FP64 matrix (x and y stay

@@ -94,18 +94,29 @@ std::vector<double> sliced_decode(const SlicedHostView& v, int64_t n_rows, const
   const double* val = static_cast<const double*>(v.val);
   for (int64_t t = 0; t < v.num_tasks; ++t) {
     const SlicedTask& tk = v.tasks[t];
-    const int kind = tk.meta & 15, vwl = (tk.meta >> 4) & 15, nrows = tk.meta >> 8;
+    const int kind = tk.meta & 15, vwl = (tk.meta >> 4) & 15, nrows = (tk.meta >> 8) & 0xff;
     if (kind == kSlicedZero) {
       for (int l = 0; l < nrows; ++l) y[(size_t)v.rowid[tk.row_base + l]] = 0.0;
       continue;
     }
     const int VW = 1 << vwl;
     double lane[32] = {0};
-    for (int s = 0; s < tk.steps; ++s)
+    if (tk.meta & kSlicedDelta) {
       for (int l = 0; l < 32; ++l) {
-        const int64_t e = (int64_t)tk.base + (int64_t)s * 32 + l;
-        lane[l] += val[e] * x[(size_t)v.col[e]];
+        int64_t c = l < nrows ? v.first[tk.row_base + l] : 0;
+        for (int s = 0; s < tk.steps; ++s) {
+          const int64_t e = (int64_t)tk.base + (int64_t)s * 32 + l;
+          c += v.col16[e];
+          lane[l] += val[e] * x[(size_t)c];
+        }
       }
+    } else {
+      for (int s = 0; s < tk.steps; ++s)
+        for (int l = 0; l < 32; ++l) {
+          const int64_t e = (int64_t)tk.base + (int64_t)s * 32 + l;
+          lane[l] += val[e] * x[(size_t)v.col[e]];
+        }
+    }
     if (kind == kSlicedChunk) {
       double sum = 0;
       for (int l = 0; l < 32; ++l) sum += lane[l];
@@ -191,6 +202,7 @@ int main() {
       prm.long_len = variant == 2 ? 32 : 1024;
       prm.chunk = variant == 2 ? 64 : 1024;
       prm.max_steps = variant == 3 ? 1 : 32;
+      prm.delta16 = variant != 1;
       // keep mask: every other row in variant 3 (the rest must stay NaN)
       std::vector<uint8_t> keep((size_t)n_rows, 1);
       if (variant == 3)

@@ -402,6 +402,25 @@ def test_sliced_host_calls_split_into_parts(built, kw):
         p.free()
 
 
+@pytest.mark.parametrize("prec", [0, 1, 2, 3], ids=["fp64", "fp32", "bf16_rowscale", "df32_hilo"])
+def test_sliced_column_deltas(built, prec):
+    """16-bit column deltas change only how columns are stored: results are
+    bit-identical to 32-bit columns (finite x), for every precision form."""
+    from vnec_gb300 import api
+    from vnec_gb300 import generators as G
+
+    for m in (G.stencil27(24, seed=3), G.banded(20000, 21, seed=2), G.uniform_k(30000, 12, seed=4),
+              G.lognormal(20000, sigma=1.0, cap=64, seed=5)):
+        xv = G.vector(m.n_cols, seed=8)
+        ys = []
+        for cd in (-1, 0):
+            p = api.Plan(m, kernel=api.KERNEL_S, precision=prec, column_deltas=cd, hot_columns=-1)
+            ys.append(p.mxv_host(xv))
+            p.free()
+        assert ys[0].tobytes() == ys[1].tobytes()
+        check_f64(ys[1], m, xv, tol=PREC_TOL.get(prec, TOL_F64))
+
+
 def test_sliced_full_size_rmat_scale24(built):
     from vnec_gb300 import api
     from vnec_gb300 import generators as G

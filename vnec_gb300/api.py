@@ -65,7 +65,8 @@ class Options(C.Structure):
                 ("pipeline_stages", C.c_int), ("arithmetic", C.c_int), ("window_rows", C.c_int),
                 ("long_row_len", C.c_int), ("max_steps", C.c_int), ("cache_hints", C.c_int),
                 ("precision", C.c_int), ("hot_columns", C.c_int), ("dense_fill_permille", C.c_int),
-                ("transpose", C.c_int), ("host_parts", C.c_int), ("reserved", C.c_int * 2)]
+                ("transpose", C.c_int), ("host_parts", C.c_int), ("column_deltas", C.c_int),
+                ("reserved", C.c_int * 1)]
 
 
 class Info(C.Structure):
@@ -351,7 +352,8 @@ def SpB_mxv(y: Vector, A: Matrix, x: Vector, vnec: int | None = None) -> None:
 def options(kernel: int = KERNEL_AUTO, threads_per_block: int = 0, items_per_thread: int = 0,
             pipeline_stages: int = 0, arithmetic: int = ARITH_AUTO, window_rows: int = 0, long_row_len: int = 0,
             max_steps: int = 0, cache_hints: int = 0, precision: int = PREC_FP64, hot_columns: int = 0,
-            dense_fill_permille: int = 0, transpose: bool = False, host_parts: int = 0) -> Options:
+            dense_fill_permille: int = 0, transpose: bool = False, host_parts: int = 0,
+            column_deltas: int = 0) -> Options:
     o = Options()
     o.kernel, o.threads_per_block, o.items_per_thread = kernel, threads_per_block, items_per_thread
     o.pipeline_stages, o.arithmetic = pipeline_stages, arithmetic
@@ -360,6 +362,7 @@ def options(kernel: int = KERNEL_AUTO, threads_per_block: int = 0, items_per_thr
     o.dense_fill_permille = dense_fill_permille
     o.transpose = int(transpose)
     o.host_parts = host_parts
+    o.column_deltas = column_deltas
     return o
 
 

@@ -16,6 +16,10 @@ namespace vnec {
 //               goes to chunk_sum[row_base] and a fix-up adds the pieces.
 //   kind ZERO : `nrows` empty rows, y[rowid[row_base + lane]] = 0.
 enum SlicedKind : int { kSlicedRows = 0, kSlicedChunk = 1, kSlicedZero = 2 };
+// meta flag of a ROWS task with VW = 1 whose columns are stored as 16-bit
+// deltas: lane g starts at first[row_base + g] and adds col16[entry] at each
+// step (0 on padding), so the column stream costs 2 bytes per entry instead of 4.
+constexpr int kSlicedDelta = 1 << 16;
 
 struct SlicedTask {
   int32_t base;      // first entry (element index into vals / cols)
@@ -45,6 +49,8 @@ struct SlicedMatrix {
   const int32_t* hot_cols = nullptr;  // original column of each slot
   void* xhot = nullptr;               // FP64 kernel: hot x values
   bool hot_ready = false;             // xhot already gathered for this call (later parts of a split call)
+  const uint16_t* col16 = nullptr;    // delta tasks (kSlicedDelta): 16-bit column deltas
+  const int32_t* first = nullptr;     // delta tasks: first column of each row slot
 };
 
 struct SlicedParams {
@@ -53,6 +59,7 @@ struct SlicedParams {
   int chunk = 1024;           // entries per chunk (multiple of 32)
   int max_steps = 32;         // target load steps per lane for grouped rows
   int hot = 0;                // hot-column window size (0: none)
+  bool delta16 = false;       // 16-bit column deltas for VW = 1 groups whose rows allow it
 };
 
 // Host-side arrays of a built sliced matrix.
@@ -77,6 +84,8 @@ struct SlicedHostView {
   const int32_t* long_row;
   const int32_t* long_first;
   int vpe;
+  const uint16_t* col16;  // delta tasks' column deltas (entries), or null
+  const int32_t* first;   // first column of each row slot (n_rowid), or null
   // Windows of window_rows rows in row order: tasks, long rows and entries of
   // window w start at win_task[w], win_long[w], win_entry[w].
   int64_t num_windows;

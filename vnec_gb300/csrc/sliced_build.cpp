@@ -31,6 +31,8 @@ struct SlicedHost {
   std::unique_ptr<unsigned char[]> val;
   std::unique_ptr<int32_t[]> col;
   std::vector<int32_t> rowid, long_row, long_first;
+  std::unique_ptr<uint16_t[]> col16;  // delta16 layouts only
+  std::vector<int32_t> first;
 };
 
 namespace {
@@ -159,6 +161,11 @@ SlicedHost* sliced_build(int64_t n_rows, int64_t n_cols, const int64_t* rp, cons
   h->vpe = vpe;
   std::memset(h->val.get() + (size_t)h->entries * eb, 0, (size_t)pad * eb);
   std::memset(h->col.get() + h->entries, 0, sizeof(int32_t) * pad);
+  if (prm.delta16) {
+    h->col16.reset(new uint16_t[(size_t)(h->entries + pad)]);
+    std::memset(h->col16.get(), 0, sizeof(uint16_t) * (size_t)(h->entries + pad));
+    h->first.assign((size_t)std::max<int64_t>(h->n_rowid, 1), 0);
+  }
 
   // Pass 2: global task list and the interleaved entries.
 #pragma omp parallel for schedule(dynamic, 1)
@@ -175,7 +182,7 @@ SlicedHost* sliced_build(int64_t n_rows, int64_t n_cols, const int64_t* rp, cons
     int64_t chunk_in_row = 0;
     for (size_t ti = 0; ti < wd.tasks.size(); ++ti) {
       SlicedTask t = wd.tasks[ti];
-      const int kind = t.meta & 15, vwl = (t.meta >> 4) & 15, nrows = t.meta >> 8;
+      const int kind = t.meta & 15, vwl = (t.meta >> 4) & 15, nrows = (t.meta >> 8) & 0xff;
       if (kind != kSlicedZero) t.base += (int32_t)off_e[w];
       if (kind == kSlicedChunk)
         t.row_base += (int32_t)off_c[w];
@@ -199,6 +206,29 @@ SlicedHost* sliced_build(int64_t n_rows, int64_t n_cols, const int64_t* rp, cons
             cdst[pos] = colat(b + j);
             std::memcpy(vdst + pos * eb, static_cast<const unsigned char*>(val) + (b + j) * eb, (size_t)eb);
           }
+        }
+        // 16-bit deltas when every row of the group has increasing columns
+        // whose gaps fit (VW = 1 groups only: one lane walks one row).
+        bool delta_ok = prm.delta16 && vwl == 0;
+        for (int g = 0; g < nrows && delta_ok; ++g) {
+          const int32_t r = h->rowid[(size_t)(t.row_base + g)];
+          for (int64_t q = begin(r) + 1; q < begin(r + 1); ++q) {
+            const int64_t d = (int64_t)colat(q) - colat(q - 1);
+            if (d <= 0 || d > 65535) {
+              delta_ok = false;
+              break;
+            }
+          }
+        }
+        if (delta_ok) {
+          uint16_t* ddst = h->col16.get() + t.base;
+          for (int g = 0; g < nrows; ++g) {
+            const int32_t r = h->rowid[(size_t)(t.row_base + g)];
+            const int64_t b = begin(r), len = begin(r + 1) - b;
+            h->first[(size_t)(t.row_base + g)] = colat(b);
+            for (int64_t j = 1; j < len; ++j) ddst[j * 32 + g] = (uint16_t)(colat(b + j) - colat(b + j - 1));
+          }
+          h->tasks[(size_t)(off_t[w] + (int64_t)ti)].meta |= kSlicedDelta;
         }
       } else {  // chunk of a long row
         const int32_t r = wd.long_row[li];
@@ -236,6 +266,8 @@ SlicedHostView sliced_view(const SlicedHost* h) {
   v.long_row = h->long_row.data();
   v.long_first = h->long_first.data();
   v.vpe = h->vpe;
+  v.col16 = h->col16.get();
+  v.first = h->first.empty() ? nullptr : h->first.data();
   v.num_windows = (int64_t)h->win_task.size() - 1;
   v.win_task = h->win_task.data();
   v.win_long = h->win_long.data();

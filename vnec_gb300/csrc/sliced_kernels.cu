@@ -148,7 +148,7 @@ dense_block_kernel(const SlicedTask* __restrict__ tasks, long long num_tasks, co
   if (w >= num_tasks) return;
   const int4 raw = __ldg(reinterpret_cast<const int4*>(tasks) + w);
   const int base = raw.x, row_base = raw.y, steps = raw.z, meta = raw.w;
-  const int kind = meta & 15, vwl = (meta >> 4) & 15, nrows = meta >> 8;
+  const int kind = meta & 15, vwl = (meta >> 4) & 15, nrows = (meta >> 8) & 0xff;
   if (kind == kSlicedZero) {
     if (lane < nrows) y[rowid[row_base + lane]] = V(0);
     return;
@@ -200,18 +200,54 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
 sliced_kernel(const SlicedTask* __restrict__ tasks, long long num_tasks, const V* __restrict__ val,
               const int32_t* __restrict__ col, const int32_t* __restrict__ rowid, const V* __restrict__ x,
               V* y, V* __restrict__ chunk_sum, const int* __restrict__ guard = nullptr,
-              const V* __restrict__ xh = nullptr, int ncols = 0, SlicedEpilogue ep = SlicedEpilogue()) {
+              const V* __restrict__ xh = nullptr, int ncols = 0, SlicedEpilogue ep = SlicedEpilogue(),
+              const uint16_t* __restrict__ col16 = nullptr, const int32_t* __restrict__ first = nullptr) {
   if (guard && *reinterpret_cast<const volatile int*>(guard) == 0) return;
   const long long w = ((long long)blockIdx.x * kWarpsPerBlock) + (threadIdx.x >> 5);
   const int lane = threadIdx.x & 31;
   if (w >= num_tasks) return;
   const int4 raw = __ldg(reinterpret_cast<const int4*>(tasks) + w);
   const int base = raw.x, row_base = raw.y, steps = raw.z, meta = raw.w;
-  const int kind = meta & 15, vwl = (meta >> 4) & 15, nrows = meta >> 8;
+  const int kind = meta & 15, vwl = (meta >> 4) & 15, nrows = (meta >> 8) & 0xff;
   if (kind == kSlicedZero) {
     if (lane < nrows) {
       const int row = rowid[row_base + lane];
       y[row] = epi_out<EPI>(V(0), row, ep);
+    }
+    return;
+  }
+  if (meta & kSlicedDelta) {
+    // One row per lane, columns as 16-bit deltas from the row's first column.
+    const V* vp = val + base + lane;
+    const uint16_t* dp = col16 + base + lane;
+    int c = lane < nrows ? __ldg(first + row_base + lane) : 0;
+    V acc = V(0);
+    int k = 0;
+    for (; k + U <= steps; k += U) {
+      int cc[U];
+      V v[U], xv[U];
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        cc[u] = __ldcs(dp + (k + u) * 32);
+        v[u] = __ldcs(vp + (k + u) * 32);
+      }
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        c += cc[u];
+        cc[u] = c;
+      }
+#pragma unroll
+      for (int u = 0; u < U; ++u) xv[u] = __ldg(x_at<HOT>(x, xh, ncols, cc[u]));
+#pragma unroll
+      for (int u = 0; u < U; ++u) acc = fmav<V>(v[u], xv[u], acc);
+    }
+    for (; k < steps; ++k) {
+      c += __ldcs(dp + k * 32);
+      acc = fmav<V>(__ldcs(vp + k * 32), __ldg(x_at<HOT>(x, xh, ncols, c)), acc);
+    }
+    if (lane < nrows) {
+      const int row = rowid[row_base + lane];
+      y[row] = epi_out<EPI>(acc, row, ep);
     }
     return;
   }
@@ -312,7 +348,8 @@ bool launch_main(const SlicedMatrix& m, const void* x, void* y, cudaStream_t s,
   kern<<<(unsigned)grid, kWarpsPerBlock * 32, 0, s>>>(m.tasks, m.num_tasks, static_cast<const V*>(m.val), m.col,
                                                       m.rowid, static_cast<const V*>(x), static_cast<V*>(y),
                                                       static_cast<V*>(m.chunk_sum), nullptr,
-                                                      static_cast<const V*>(m.xhot), (int)m.n_cols, ep);
+                                                      static_cast<const V*>(m.xhot), (int)m.n_cols, ep, m.col16,
+                                                      m.first);
   return VNEC_CUDA(cudaGetLastError());
 }
 
@@ -388,11 +425,12 @@ bool sliced_guard_f64(const SlicedMatrix& m, const double* x, double* y, const i
     if (!VNEC_CUDA(cudaGetLastError())) return false;
     sliced_kernel<double, 8, 0, true><<<(unsigned)grid, kWarpsPerBlock * 32, 0, s>>>(
         m.tasks, m.num_tasks, static_cast<const double*>(m.val), m.col, m.rowid, x, y,
-        static_cast<double*>(m.chunk_sum), flag, static_cast<const double*>(m.xhot), (int)m.n_cols);
+        static_cast<double*>(m.chunk_sum), flag, static_cast<const double*>(m.xhot), (int)m.n_cols,
+        SlicedEpilogue(), m.col16, m.first);
   } else {
     sliced_kernel<double, 8, 0><<<(unsigned)grid, kWarpsPerBlock * 32, 0, s>>>(
         m.tasks, m.num_tasks, static_cast<const double*>(m.val), m.col, m.rowid, x, y,
-        static_cast<double*>(m.chunk_sum), flag);
+        static_cast<double*>(m.chunk_sum), flag, nullptr, 0, SlicedEpilogue(), m.col16, m.first);
   }
   return VNEC_CUDA(cudaGetLastError());
 }

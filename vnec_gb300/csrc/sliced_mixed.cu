@@ -190,16 +190,48 @@ __global__ void __launch_bounds__(kWarps * 32)
 sliced_mixed_kernel(const SlicedTask* __restrict__ tasks, long long num_tasks, const typename C::Val* __restrict__ val,
                     const int32_t* __restrict__ col, const int32_t* __restrict__ rowid, const void* __restrict__ xs,
                     double* __restrict__ y, double* __restrict__ chunk_sum, const signed char* __restrict__ row_scale,
-                    const signed char* __restrict__ chunk_scale, const int* __restrict__ flag) {
+                    const signed char* __restrict__ chunk_scale, const int* __restrict__ flag,
+                    const uint16_t* __restrict__ col16, const int32_t* __restrict__ first) {
   if (flag && *reinterpret_cast<const volatile int*>(flag)) return;  // DF32: x out of range, guard launch computes
   const long long w = ((long long)blockIdx.x * kWarps) + (threadIdx.x >> 5);
   const int lane = threadIdx.x & 31;
   if (w >= num_tasks) return;
   const int4 raw = __ldg(reinterpret_cast<const int4*>(tasks) + w);
   const int base = raw.x, row_base = raw.y, steps = raw.z, meta = raw.w;
-  const int kind = meta & 15, vwl = (meta >> 4) & 15, nrows = meta >> 8;
+  const int kind = meta & 15, vwl = (meta >> 4) & 15, nrows = (meta >> 8) & 0xff;
   if (kind == kSlicedZero) {
     if (lane < nrows) y[rowid[row_base + lane]] = 0.0;
+    return;
+  }
+  if (meta & kSlicedDelta) {
+    // One row per lane, columns as 16-bit deltas from the row's first column.
+    const typename C::Val* vp = val + base + lane;
+    const uint16_t* dp = col16 + base + lane;
+    int c = lane < nrows ? __ldg(first + row_base + lane) : 0;
+    typename C::Acc acc = C::zero();
+    int k = 0;
+    for (; k + U <= steps; k += U) {
+      int cc[U];
+      typename C::Val v[U];
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        cc[u] = __ldcs(dp + (k + u) * 32);
+        v[u] = ld_stream(vp + (k + u) * 32);
+      }
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        c += cc[u];
+        acc = C::mac(acc, v[u], xs, c);
+      }
+    }
+    for (; k < steps; ++k) {
+      c += __ldcs(dp + k * 32);
+      acc = C::mac(acc, ld_stream(vp + k * 32), xs, c);
+    }
+    if (lane < nrows) {
+      const double s = C::to_f64(acc);
+      y[rowid[row_base + lane]] = row_scale ? s * pow2(row_scale[row_base + lane]) : s;
+    }
     return;
   }
   const typename C::Val* vp = val + base + lane;
@@ -256,7 +288,7 @@ bool launch_mixed(const SlicedMatrix& m, const SlicedMixed& mx, const void* xs, 
                                : sliced_mixed_kernel<C, 8>;
   kern<<<(unsigned)grid, kWarps * 32, 0, s>>>(m.tasks, m.num_tasks, static_cast<const typename C::Val*>(m.val), m.col,
                                               m.rowid, xs, y, static_cast<double*>(m.chunk_sum), mx.row_scale,
-                                              mx.chunk_scale, flag);
+                                              mx.chunk_scale, flag, m.col16, m.first);
   return VNEC_CUDA(cudaGetLastError());
 }
 

@@ -16,7 +16,7 @@ struct SlicedPlan final : Plan {
   SlicedMatrix m;
   SlicedMixed mx;  // precision form (FP64 = plain)
   DeviceBuffer tasks, val, col, rowid, long_row, long_first, chunk_sum, xbuf, flag, row_scale, chunk_scale;
-  DeviceBuffer hot_cols, xhot;
+  DeviceBuffer hot_cols, xhot, col16, first;
   std::vector<int32_t> hot_host;  // hot-column window: original column of each slot
   SlicedParams prm;
   int64_t blocks = 0;  // dense-block plans: number of blocks of 4
@@ -164,7 +164,7 @@ struct SlicedPlan final : Plan {
   int64_t device_bytes() const override {
     return (int64_t)(tasks.bytes + val.bytes + col.bytes + rowid.bytes + long_row.bytes + long_first.bytes +
                      chunk_sum.bytes + xbuf.bytes + flag.bytes + row_scale.bytes + chunk_scale.bytes + dx.bytes +
-                     dy.bytes + hot_cols.bytes + xhot.bytes);
+                     dy.bytes + hot_cols.bytes + xhot.bytes + col16.bytes + first.bytes);
   }
   int64_t algorithmic_bytes() const override {
     // Stored value size of the form; x and y stay in the matrix's type.
@@ -321,6 +321,13 @@ std::unique_ptr<Plan> upload(std::unique_ptr<SlicedPlan> p, SlicedHost* h, int v
     p->mx.row_scale = p->row_scale.as<signed char>();
     p->mx.chunk_scale = p->chunk_scale.as<signed char>();
   }
+  if (hv.col16) {
+    if (!up(p->col16, hv.col16, sizeof(uint16_t) * (size_t)(hv.entries + pad), 0) ||
+        !up(p->first, hv.first, sizeof(int32_t) * (size_t)std::max<int64_t>(hv.n_rowid, 1), 0))
+      return nullptr;
+    p->m.col16 = p->col16.as<uint16_t>();
+    p->m.first = p->first.as<int32_t>();
+  }
   SlicedMatrix& m = p->m;
   m.n_rows = p->n_rows;
   m.n_cols = p->n_cols;
@@ -440,6 +447,9 @@ std::unique_ptr<Plan> build_sliced(const CsrView& v, const SpB_VNEC_options_ext*
     cols64 = nullptr;
     p->prm.hot = (int)p->hot_host.size();
   }
+  // 16-bit column deltas where rows allow them (not with a hot window, whose
+  // relabelled columns break the increasing order).
+  p->prm.delta16 = p->prm.hot == 0 && !(opts && opts->column_deltas < 0);
   SlicedHost* h = sliced_build(v.n_rows, v.n_cols, v.ptr, v.ptr64, cols, cols64, src_val, vb, p->prm, 1, keep);
   if (!h) {
     set_error("sliced format: more than 2^31 entries or row slots");
