@@ -102,7 +102,7 @@ SpB_VNEC_options_ext config_options(int i, const SpB_VNEC_options_ext* base) {
     o.pipeline_stages = c.chunk == 4 ? 1 : 2;
   } else {
     o.threads_per_block = 0;
-    o.items_per_thread = 0;
+    o.items_per_thread = -1;  // sliced parts time their unroll on the matrix
     o.long_row_len = c.chunk;
     o.dense_fill_permille = c.permille;
   }
