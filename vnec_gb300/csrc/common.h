@@ -5,6 +5,7 @@
 #include <cstddef>
 #include <atomic>
 #include <cstdint>
+#include <cstring>
 #include <string>
 
 namespace vnec {
@@ -36,6 +37,31 @@ bool once_per_device(std::atomic<unsigned long long>& mask, F set) {
   if (!set()) return false;
   mask.fetch_or(bit, std::memory_order_acq_rel);
   return true;
+}
+
+// Truncation split of an FP64 value into FP32 hi (sign, exponent, top 23
+// mantissa bits) and lo (the remaining 29 bits, normalised and truncated to
+// 24): the host twin of the device split used for X, so that values and X of
+// the DF32 form are split the same way.  Needs a zero or |v| in [2^-40, 2^41).
+inline void split_df_host(double v, float* hi, float* lo) {
+  uint64_t b;
+  std::memcpy(&b, &v, 8);
+  const uint32_t sign = (uint32_t)(b >> 63) << 31;
+  const int e = (int)((b >> 52) & 0x7ff);
+  const uint64_t m = b & 0xFFFFFFFFFFFFFull;
+  if (e == 0 && m == 0) {
+    *hi = 0.f;
+    *lo = 0.f;
+    return;
+  }
+  const int E = e - 1023;
+  const uint32_t hb = sign | ((uint32_t)(E + 127) << 23) | (uint32_t)(m >> 29);
+  const uint32_t rem = (uint32_t)(m & 0x1FFFFFFFull);
+  const int msb = 31 - __builtin_clz(rem | 1u);
+  const uint32_t mant = msb > 23 ? (rem >> (msb - 23)) : (rem << (23 - msb));
+  const uint32_t lb = rem ? (sign | ((uint32_t)(E - 52 + msb + 127) << 23) | (mant & 0x7FFFFFu)) : 0u;
+  std::memcpy(hi, &hb, 4);
+  std::memcpy(lo, &lb, 4);
 }
 
 struct DeviceBuffer {

@@ -118,6 +118,7 @@ struct SlicedMixed {
   int* flag = nullptr;                     // DF32: x outside the split range this call
   const signed char* row_scale = nullptr;  // BF16: power-of-two exponent per row slot
   const signed char* chunk_scale = nullptr;  // BF16: exponent per chunk
+  const float2* val_split = nullptr;         // DF32: values as FP32 (hi, lo) truncation-split pairs
 };
 bool sliced_mixed_spmv(const SlicedMatrix& m, const SlicedMixed& mx, const double* x, double* y, cudaStream_t s,
                        cudaEvent_t* events = nullptr);

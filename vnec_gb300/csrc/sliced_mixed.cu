@@ -24,6 +24,7 @@
 
 #include <algorithm>
 #include <cstdint>
+#include <type_traits>
 
 #include "common.h"
 #include "sliced.h"
@@ -158,12 +159,11 @@ struct CodecBF16 {
 };
 
 struct CodecDF32 {
-  using Val = double;
+  using Val = float2;  // (hi, lo) split at plan build (the range was checked there)
   using Acc = DF;
   __device__ static Acc zero() { return DF{0.0f, 0.0f}; }
-  __device__ static Acc mac(Acc acc, Val a, const void* xs, int c) {
-    float ah, al;
-    split_df(a, ah, al);  // A's range was checked when the plan was built
+  __device__ static Acc mac(Acc acc, Val v, const void* xs, int c) {
+    const float ah = v.x, al = v.y;
     const float2 x = __ldg(static_cast<const float2*>(xs) + c);
     const float p = __fmul_rn(ah, x.x);
     const float e = fmaf(ah, x.x, -p);              // ah*xh = p + e exactly
@@ -286,7 +286,9 @@ bool launch_mixed(const SlicedMatrix& m, const SlicedMixed& mx, const void* xs, 
               : m.unroll == 12 ? sliced_mixed_kernel<C, 12>
               : m.unroll == 16 ? sliced_mixed_kernel<C, 16>
                                : sliced_mixed_kernel<C, 8>;
-  kern<<<(unsigned)grid, kWarps * 32, 0, s>>>(m.tasks, m.num_tasks, static_cast<const typename C::Val*>(m.val), m.col,
+  // DF32 reads the pre-split (hi, lo) pairs; the FP64 values stay for the guard launch.
+  const void* vals = std::is_same<typename C::Val, float2>::value ? static_cast<const void*>(mx.val_split) : m.val;
+  kern<<<(unsigned)grid, kWarps * 32, 0, s>>>(m.tasks, m.num_tasks, static_cast<const typename C::Val*>(vals), m.col,
                                               m.rowid, xs, y, static_cast<double*>(m.chunk_sum), mx.row_scale,
                                               mx.chunk_scale, flag, m.col16, m.first);
   return VNEC_CUDA(cudaGetLastError());

@@ -16,7 +16,7 @@ struct SlicedPlan final : Plan {
   SlicedMatrix m;
   SlicedMixed mx;  // precision form (FP64 = plain)
   DeviceBuffer tasks, val, col, rowid, long_row, long_first, chunk_sum, xbuf, flag, row_scale, chunk_scale;
-  DeviceBuffer hot_cols, xhot, col16, first;
+  DeviceBuffer hot_cols, xhot, col16, first, val_split;
   std::vector<int32_t> hot_host;  // hot-column window: original column of each slot
   SlicedParams prm;
   int64_t blocks = 0;  // dense-block plans: number of blocks of 4
@@ -164,7 +164,7 @@ struct SlicedPlan final : Plan {
   int64_t device_bytes() const override {
     return (int64_t)(tasks.bytes + val.bytes + col.bytes + rowid.bytes + long_row.bytes + long_first.bytes +
                      chunk_sum.bytes + xbuf.bytes + flag.bytes + row_scale.bytes + chunk_scale.bytes + dx.bytes +
-                     dy.bytes + hot_cols.bytes + xhot.bytes + col16.bytes + first.bytes);
+                     dy.bytes + hot_cols.bytes + xhot.bytes + col16.bytes + first.bytes + val_split.bytes);
   }
   int64_t algorithmic_bytes() const override {
     // Stored value size of the form; x and y stay in the matrix's type.
@@ -320,6 +320,16 @@ std::unique_ptr<Plan> upload(std::unique_ptr<SlicedPlan> p, SlicedHost* h, int v
     if (!up(p->row_scale, rs.data(), rs.size(), 0) || !up(p->chunk_scale, cs.data(), cs.size(), 0)) return nullptr;
     p->mx.row_scale = p->row_scale.as<signed char>();
     p->mx.chunk_scale = p->chunk_scale.as<signed char>();
+  }
+  if (prec == kPrecDF32) {
+    // (hi, lo) pairs of the FP64 entries for the double-float kernel.
+    const double* src = static_cast<const double*>(hv.val);
+    const int64_t ne = hv.entries + (int64_t)pad;
+    std::vector<float> split((size_t)ne * 2);
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < ne; ++i) split_df_host(src[i], &split[2 * (size_t)i], &split[2 * (size_t)i + 1]);
+    if (!up(p->val_split, split.data(), sizeof(float) * split.size(), 0)) return nullptr;
+    p->mx.val_split = p->val_split.as<float2>();
   }
   if (hv.col16) {
     if (!up(p->col16, hv.col16, sizeof(uint16_t) * (size_t)(hv.entries + pad), 0) ||
