@@ -284,11 +284,13 @@ bool autotune(const BatchSource& s, int k, int precision, const SpB_VNEC_batch_o
   if (o->warps_per_block > 0) wpb_c = {o->warps_per_block};
   if (o->unroll > 0) deep_c = {o->unroll - 1};
   const std::vector<int> pick = tune_sample(s, (int64_t)48 << 20);
-  cudaStream_t st = nullptr;
-  cudaEvent_t e0 = nullptr, e1 = nullptr;
-  if (!VNEC_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking)) || !VNEC_CUDA(cudaEventCreate(&e0)) ||
-      !VNEC_CUDA(cudaEventCreate(&e1)))
+  TimingStream ts;
+  if (!ts.create()) {
+    set_error("batch autotune: cannot create a stream or events");
     return false;
+  }
+  cudaStream_t st = ts.s;
+  cudaEvent_t e0 = ts.e0, e1 = ts.e1;
   DeviceBuffer X, Y;
   bool ok = true;
   for (int L : lanes_c) {
@@ -337,9 +339,6 @@ bool autotune(const BatchSource& s, int k, int precision, const SpB_VNEC_batch_o
     }
     if (!ok) break;
   }
-  cudaEventDestroy(e0);
-  cudaEventDestroy(e1);
-  cudaStreamDestroy(st);
   if (!ok) return false;
   for (size_t i = 0; i < run->ms.size(); ++i)
     if (run->best < 0 || run->ms[i] < run->ms[(size_t)run->best]) run->best = (int)i;

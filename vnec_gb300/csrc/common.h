@@ -64,6 +64,25 @@ inline void split_df_host(double v, float* hi, float* lo) {
   std::memcpy(lo, &lb, 4);
 }
 
+// A non-blocking stream and two timing events, released on every exit path
+// (the timing loops of the autotuners).
+struct TimingStream {
+  cudaStream_t s = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  TimingStream() = default;
+  TimingStream(const TimingStream&) = delete;
+  TimingStream& operator=(const TimingStream&) = delete;
+  ~TimingStream() {
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    if (s) cudaStreamDestroy(s);
+  }
+  bool create() {
+    return cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) == cudaSuccess && cudaEventCreate(&e0) == cudaSuccess &&
+           cudaEventCreate(&e1) == cudaSuccess;
+  }
+};
+
 struct DeviceBuffer {
   void* ptr = nullptr;
   size_t bytes = 0;

@@ -49,12 +49,11 @@ struct SlicedPlan final : Plan {
   bool tune_unroll() {
     const size_t vb = type == SpB_FP64 ? 8 : 4;
     DeviceBuffer tx, ty;
-    cudaStream_t s = nullptr;
-    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    TimingStream ts;
     bool ok = tx.alloc(vb * (size_t)std::max<int64_t>(n_cols, 1)) && ty.alloc(vb * (size_t)std::max<int64_t>(n_rows, 1)) &&
-              VNEC_CUDA(cudaMemset(tx.ptr, 0x3f, tx.bytes)) &&
-              VNEC_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking)) && VNEC_CUDA(cudaEventCreate(&e0)) &&
-              VNEC_CUDA(cudaEventCreate(&e1));
+              VNEC_CUDA(cudaMemset(tx.ptr, 0x3f, tx.bytes)) && ts.create();
+    cudaStream_t s = ts.s;
+    cudaEvent_t e0 = ts.e0, e1 = ts.e1;
     float best = 0.f;
     int best_u = 12;
     for (int u : {4, 8, 12, 16}) {
@@ -75,9 +74,7 @@ struct SlicedPlan final : Plan {
       }
     }
     m.unroll = best_u;
-    if (e0) cudaEventDestroy(e0);
-    if (e1) cudaEventDestroy(e1);
-    if (s) cudaStreamDestroy(s);
+    if (!ok && last_error()[0] == '\0') set_error("sliced: unroll timing failed");
     return ok;
   }
   bool ensure_part_streams() {

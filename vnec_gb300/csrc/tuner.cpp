@@ -120,25 +120,26 @@ int autotune_search(const CsrView& v, const SpB_VNEC_options_ext* base, int reps
   const size_t vb = v.value_bytes();
   DeviceBuffer dx, dy, flush;
   const size_t flush_bytes = (size_t)256 << 20;
-  cudaStream_t s = nullptr;
-  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  TimingStream ts;
   int best = -1;
   if (!dx.alloc(vb * (size_t)std::max<int64_t>(v.n_cols, 1)) || !dy.alloc(vb * (size_t)std::max<int64_t>(v.n_rows, 1)) ||
-      !flush.alloc(flush_bytes) || !VNEC_CUDA(cudaMemset(dx.ptr, 0x3f, dx.bytes)) ||
-      !VNEC_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking)) || !VNEC_CUDA(cudaEventCreate(&e0)) ||
-      !VNEC_CUDA(cudaEventCreate(&e1)))
+      !flush.alloc(flush_bytes) || !VNEC_CUDA(cudaMemset(dx.ptr, 0x3f, dx.bytes))) {
+    for (int i = 0; i < kNumConfigs; ++i) ms[i] = FLT_MAX;
     return -1;
+  }
+  if (!ts.create()) {
+    set_error("autotune: cannot create a stream or events");
+    for (int i = 0; i < kNumConfigs; ++i) ms[i] = FLT_MAX;
+    return -1;
+  }
   for (int i = 0; i < kNumConfigs; ++i) {
     ms[i] = FLT_MAX;
     if (!available(i, v, sorted)) continue;
     std::unique_ptr<Plan> p = build_config(i, v, base);
     if (!p) continue;
-    ms[i] = time_plan(p.get(), dx.ptr, dy.ptr, flush.ptr, flush_bytes, reps, s, e0, e1);
+    ms[i] = time_plan(p.get(), dx.ptr, dy.ptr, flush.ptr, flush_bytes, reps, ts.s, ts.e0, ts.e1);
     if (ms[i] < FLT_MAX && (best < 0 || ms[i] < ms[best])) best = i;
   }
-  cudaEventDestroy(e0);
-  cudaEventDestroy(e1);
-  cudaStreamDestroy(s);
   if (best < 0) set_error("autotune: no configuration could be built");
   return best;
 }
