@@ -158,7 +158,10 @@ typedef struct {
   int column_deltas;     /* sliced: store the columns of one-row-per-lane groups as 16-bit
                             deltas where the gaps allow (0: on unless a hot-column window
                             is used, -1: off) */
-  int reserved[1];
+  int lane_vectors;      /* sliced FP32 form: each lane's entries stored in runs of 4
+                            consecutive steps, read as 16-byte vectors (0: where most
+                            entries use 16-bit column deltas, 1: on, -1: off; the sums
+                            are the same either way) */
 } SpB_VNEC_options_ext;
 
 /* Precision forms of the sliced kernel for an FP64 matrix (x and y stay

@@ -421,6 +421,31 @@ def test_sliced_column_deltas(built, prec):
         check_f64(ys[1], m, xv, tol=PREC_TOL.get(prec, TOL_F64))
 
 
+@pytest.mark.parametrize("kw", [dict(), dict(column_deltas=-1), dict(hot_columns=2048),
+                                dict(long_row_len=64, max_steps=7), dict(unroll=4), dict(unroll=8),
+                                dict(unroll=16)],
+                         ids=["deltas", "cols", "hot", "chunks_odd_steps", "u4", "u8", "u16"])
+def test_sliced_lane_vectors(built, kw):
+    """FP32 lane runs (each lane's consecutive entries side by side, read as
+    16-byte vectors) change only the storage order: y is bit-identical to the
+    stride-32 layout, with whole runs, ragged tails, chunks and wide row groups."""
+    from vnec_gb300 import api
+    from vnec_gb300 import generators as G
+
+    kw = dict(kw)
+    u = kw.pop("unroll", 12)
+    for m in (G.stencil27(20, seed=3), G.banded(20000, 13, seed=2), G.lognormal(20000, sigma=1.3, cap=900, seed=5),
+              G.rmat(14, 1 << 18, seed=6), _edge_matrix("hub_rows_and_empties")):
+        xv = G.vector(m.n_cols, seed=8)
+        ys = []
+        for lv in (-1, 1):
+            p = api.Plan(m, kernel=api.KERNEL_S, precision=1, lane_vectors=lv, items_per_thread=u, **kw)
+            ys.append(p.mxv_host(xv))
+            p.free()
+        assert ys[0].tobytes() == ys[1].tobytes()
+        check_f64(ys[1], m, xv, tol=PREC_TOL[1])
+
+
 def test_sliced_full_size_rmat_scale24(built):
     from vnec_gb300 import api
     from vnec_gb300 import generators as G

@@ -181,11 +181,47 @@ template <> __device__ __forceinline__ unsigned short ld_stream<unsigned short>(
   return __ldcs(p);
 }
 
+// One lane run (SlicedMatrix::lane_run): N consecutive 32-bit words read as
+// streaming 8- or 16-byte vectors.
+template <int N>
+__device__ __forceinline__ void ld_words(const void* p, uint32_t (&w)[N]) {
+  static_assert(N == 2 || N % 4 == 0, "runs are 8 bytes or whole 16-byte vectors");
+  if constexpr (N == 2) {
+    const uint2 r = __ldcs(static_cast<const uint2*>(p));
+    w[0] = r.x;
+    w[1] = r.y;
+  } else {
+#pragma unroll
+    for (int i = 0; i < N / 4; ++i) {
+      const uint4 r = __ldcs(static_cast<const uint4*>(p) + i);
+      w[4 * i] = r.x;
+      w[4 * i + 1] = r.y;
+      w[4 * i + 2] = r.z;
+      w[4 * i + 3] = r.w;
+    }
+  }
+}
+// Element t of a run of 4-byte (float, int32) or 2-byte (BF16, delta) items.
+template <typename T, int N>
+__device__ __forceinline__ T run_at(const uint32_t (&w)[N], int t) {
+  if constexpr (sizeof(T) == 4) {
+    T v;
+    memcpy(&v, &w[t], 4);
+    return v;
+  } else {
+    static_assert(sizeof(T) == 2, "2- or 4-byte items");
+    return static_cast<T>((w[t >> 1] >> (16 * (t & 1))) & 0xffffu);
+  }
+}
+
 __device__ __forceinline__ double pow2(int e) {
   return __longlong_as_double(static_cast<long long>(e + 1023) << 52);
 }
 
-template <class C, int U>
+// P > 0: the arrays hold lane runs of P steps (SlicedMatrix::lane_run);
+// 2U / P runs are in flight per lane.  The per-lane sums take the same steps
+// in the same order as the stride-32 layout (P = 0), so both give the same y.
+template <class C, int U, int P>
 __global__ void __launch_bounds__(kWarps * 32)
 sliced_mixed_kernel(const SlicedTask* __restrict__ tasks, long long num_tasks, const typename C::Val* __restrict__ val,
                     const int32_t* __restrict__ col, const int32_t* __restrict__ rowid, const void* __restrict__ xs,
@@ -203,12 +239,62 @@ sliced_mixed_kernel(const SlicedTask* __restrict__ tasks, long long num_tasks, c
     if (lane < nrows) y[rowid[row_base + lane]] = 0.0;
     return;
   }
+  using Val = typename C::Val;
+  // Lane runs: rounds of 2U steps (2U / P runs) per lane, the ragged tail
+  // loaded with the first round and summed last.
+  constexpr int UB = P > 0 ? 2 * U / P : 1;                  // runs per round
+  constexpr int VW = P > 0 ? P * (int)sizeof(Val) / 4 : 1;  // words per value run
+  constexpr int TL = P > 1 ? P - 1 : 1;                      // stride-32 steps after the runs
   if (meta & kSlicedDelta) {
     // One row per lane, columns as 16-bit deltas from the row's first column.
-    const typename C::Val* vp = val + base + lane;
+    const Val* vp = val + base + lane;
     const uint16_t* dp = col16 + base + lane;
     int c = lane < nrows ? __ldg(first + row_base + lane) : 0;
     typename C::Acc acc = C::zero();
+    if constexpr (P > 0) {
+      constexpr int DW = P / 2;  // words per delta run
+      const int nb = steps / P, k0 = nb * P;
+      const int row = lane < nrows ? __ldg(rowid + row_base + lane) : 0;
+      int dd[TL];
+      Val tv[TL];
+#pragma unroll
+      for (int t = 0; t < TL; ++t)
+        if (k0 + t < steps) {
+          dd[t] = __ldcs(dp + (k0 + t) * 32);
+          tv[t] = ld_stream(vp + (k0 + t) * 32);
+        }
+      const Val* vr = val + base + lane * P;
+      const uint16_t* dr = col16 + base + lane * P;
+      for (int b = 0; b < nb; b += UB) {
+        uint32_t vw[UB][VW], dw[UB][DW];
+#pragma unroll
+        for (int u = 0; u < UB; ++u)
+          if (b + u < nb) {
+            ld_words(dr + (b + u) * 32 * P, dw[u]);
+            ld_words(vr + (b + u) * 32 * P, vw[u]);
+          }
+#pragma unroll
+        for (int u = 0; u < UB; ++u)
+          if (b + u < nb) {
+#pragma unroll
+            for (int t = 0; t < P; ++t) {
+              c += run_at<uint16_t>(dw[u], t);
+              acc = C::mac(acc, run_at<Val>(vw[u], t), xs, c);
+            }
+          }
+      }
+#pragma unroll
+      for (int t = 0; t < TL; ++t)
+        if (k0 + t < steps) {
+          c += dd[t];
+          acc = C::mac(acc, tv[t], xs, c);
+        }
+      if (lane < nrows) {
+        const double s = C::to_f64(acc);
+        y[row] = row_scale ? s * pow2(row_scale[row_base + lane]) : s;
+      }
+      return;
+    }
     int k = 0;
     for (; k + U <= steps; k += U) {
       int cc[U];
@@ -234,10 +320,42 @@ sliced_mixed_kernel(const SlicedTask* __restrict__ tasks, long long num_tasks, c
     }
     return;
   }
-  const typename C::Val* vp = val + base + lane;
+  const Val* vp = val + base + lane;
   const int32_t* cp = col + base + lane;
   typename C::Acc acc = C::zero();
   int k = 0;
+  if constexpr (P > 0) {
+    const int nb = steps / P, k0 = nb * P;
+    int tc[TL];
+    Val tv[TL];
+#pragma unroll
+    for (int t = 0; t < TL; ++t)
+      if (k0 + t < steps) {
+        tc[t] = __ldcs(cp + (k0 + t) * 32);
+        tv[t] = ld_stream(vp + (k0 + t) * 32);
+      }
+    const Val* vr = val + base + lane * P;
+    const int32_t* cr = col + base + lane * P;
+    for (int b = 0; b < nb; b += UB) {
+      uint32_t vw[UB][VW], cw[UB][P];
+#pragma unroll
+      for (int u = 0; u < UB; ++u)
+        if (b + u < nb) {
+          ld_words(cr + (b + u) * 32 * P, cw[u]);
+          ld_words(vr + (b + u) * 32 * P, vw[u]);
+        }
+#pragma unroll
+      for (int u = 0; u < UB; ++u)
+        if (b + u < nb) {
+#pragma unroll
+          for (int t = 0; t < P; ++t) acc = C::mac(acc, run_at<Val>(vw[u], t), xs, (int)cw[u][t]);
+        }
+    }
+#pragma unroll
+    for (int t = 0; t < TL; ++t)
+      if (k0 + t < steps) acc = C::mac(acc, tv[t], xs, tc[t]);
+    k = steps;
+  }
   for (; k + U <= steps; k += U) {
     int c[U];
     typename C::Val v[U];
@@ -282,10 +400,20 @@ bool launch_mixed(const SlicedMatrix& m, const SlicedMixed& mx, const void* xs, 
     set_error("sliced: too many tasks for one launch");
     return false;
   }
-  auto kern = m.unroll == 4    ? sliced_mixed_kernel<C, 4>
-              : m.unroll == 12 ? sliced_mixed_kernel<C, 12>
-              : m.unroll == 16 ? sliced_mixed_kernel<C, 16>
-                               : sliced_mixed_kernel<C, 8>;
+  // Lane runs (FP32 form): 4 steps, 16 bytes of values.
+  constexpr int R = std::is_same<typename C::Val, float>::value ? 4 : 0;
+  if (m.lane_run != 0 && m.lane_run != R) {
+    set_error("sliced: lane runs do not match the precision form");
+    return false;
+  }
+  auto pick = [&](auto run) {
+    constexpr int P = decltype(run)::value;
+    return m.unroll == 4    ? sliced_mixed_kernel<C, 4, P>
+           : m.unroll == 12 ? sliced_mixed_kernel<C, 12, P>
+           : m.unroll == 16 ? sliced_mixed_kernel<C, 16, P>
+                            : sliced_mixed_kernel<C, 8, P>;
+  };
+  auto kern = (R > 0 && m.lane_run) ? pick(std::integral_constant<int, R>{}) : pick(std::integral_constant<int, 0>{});
   // DF32 reads the pre-split (hi, lo) pairs; the FP64 values stay for the guard launch.
   const void* vals = std::is_same<typename C::Val, float2>::value ? static_cast<const void*>(mx.val_split) : m.val;
   kern<<<(unsigned)grid, kWarps * 32, 0, s>>>(m.tasks, m.num_tasks, static_cast<const typename C::Val*>(vals), m.col,
