@@ -205,6 +205,18 @@ SpB_Info SpB_mxv_axpby_ext(void *plan, const void *d_x, void *d_y, double alpha,
 /* y := A x with host x and y (the SpB_mxv data path without SpB_Vector). */
 SpB_Info SpB_mxv_host_ext(void *plan, const void *h_x, void *h_y);
 
+/* Pipelined host-vector calls for a stream of independent right-hand sides:
+ * enqueues y := A x (copy x in, SpMV, copy y out) and returns without waiting.
+ * Each call uses one of two device buffer slots; its x copy overlaps the
+ * previous call's SpMV and its y copy the next call's, so a sequence of
+ * calls runs at the rate of its slowest stage.  h_x must not change and h_y
+ * must not be read until SpB_VNEC_host_wait_ext returns; page-locked host
+ * buffers are needed for the copies to overlap.  Works with every plan kind. */
+SpB_Info SpB_mxv_host_async_ext(void *plan, const void *h_x, void *h_y);
+/* Waits for every enqueued pipelined call of the plan and reports device-side
+ * errors (as SpB_VNEC_device_status_ext). */
+SpB_Info SpB_VNEC_host_wait_ext(void *plan);
+
 /* Plan description. */
 typedef struct {
   int kernel;              /* SpB_VNEC_kernel_ext actually built */

@@ -129,6 +129,10 @@ def lib() -> C.CDLL:
     L.SpB_mxv_axpby_ext.restype = C.c_int
     L.SpB_mxv_host_ext.argtypes = [_vp, _vp, _vp]
     L.SpB_mxv_host_ext.restype = C.c_int
+    L.SpB_mxv_host_async_ext.argtypes = [_vp, _vp, _vp]
+    L.SpB_mxv_host_async_ext.restype = C.c_int
+    L.SpB_VNEC_host_wait_ext.argtypes = [_vp]
+    L.SpB_VNEC_host_wait_ext.restype = C.c_int
     L.SpB_VNEC_plan_info_ext.argtypes = [_vp, C.POINTER(Info)]
     L.SpB_VNEC_plan_info_ext.restype = C.c_int
     L.SpB_VNEC_set_profiling_ext.argtypes = [_vp, C.c_int]
@@ -410,6 +414,18 @@ class Plan:
             y = np.empty(inf_rows, dtype=self.dtype)
         _check(lib().SpB_mxv_host_ext(self.h, x.ctypes.data, y.ctypes.data) == SpB_SUCCESS, "SpB_mxv_host_ext")
         return y
+
+    def mxv_host_async(self, x: np.ndarray, y: np.ndarray) -> None:
+        """Enqueues y := A x on the pipelined host path (SpB_mxv_host_async_ext);
+        x and y must be contiguous arrays of the plan's type that stay alive and
+        untouched until host_wait() returns."""
+        if x.dtype != self.dtype or y.dtype != self.dtype or not (x.flags.c_contiguous and y.flags.c_contiguous):
+            raise ValueError("x and y must be contiguous arrays of the plan's value type")
+        _check(lib().SpB_mxv_host_async_ext(self.h, x.ctypes.data, y.ctypes.data) == SpB_SUCCESS,
+               "SpB_mxv_host_async_ext")
+
+    def host_wait(self) -> None:
+        _check(lib().SpB_VNEC_host_wait_ext(self.h) == SpB_SUCCESS, "SpB_VNEC_host_wait_ext")
 
     def spmspv_host(self, idx: np.ndarray, val: np.ndarray, y: np.ndarray | None = None) -> np.ndarray:
         """y = A x for sparse x (push plans): idx int32 positions, val values."""

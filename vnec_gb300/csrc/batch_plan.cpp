@@ -431,6 +431,12 @@ struct BatchPlan final : Plan {
            device_status(own_stream);
   }
 
+  // Pipelined host calls alternate two buffer slots: direct launches (one or
+  // two kernels) instead of re-pointing the graph on every call.
+  bool run_slot(int, const void* d_x, void* d_y, cudaStream_t s) override {
+    return batch_spmm(d.m, static_cast<const double*>(d_x), static_cast<double*>(d_y), s);
+  }
+
   bool capture(const void* d_x, void* d_y) {
     if (!cap && !VNEC_CUDA(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking))) return false;
     if (!VNEC_CUDA(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal))) return false;

@@ -538,6 +538,30 @@ SpB_Info SpB_mxv_host_ext(void* plan, const void* h_x, void* h_y) {
   return p->run_host(h_x, h_y) ? SpB_SUCCESS : SpB_FAILURE;
 }
 
+SpB_Info SpB_mxv_host_async_ext(void* plan, const void* h_x, void* h_y) {
+  clear_error();
+  Plan* p = find_plan(plan);
+  if (!p) {
+    set_error("unknown plan");
+    return SpB_FAILURE;
+  }
+  if ((p->n_cols > 0 && !h_x) || (p->n_rows > 0 && !h_y)) {
+    set_error("x or y is NULL");
+    return SpB_FAILURE;
+  }
+  return p->run_host_async(h_x, h_y) ? SpB_SUCCESS : SpB_FAILURE;
+}
+
+SpB_Info SpB_VNEC_host_wait_ext(void* plan) {
+  clear_error();
+  Plan* p = find_plan(plan);
+  if (!p) {
+    set_error("unknown plan");
+    return SpB_FAILURE;
+  }
+  return p->host_wait() ? SpB_SUCCESS : SpB_FAILURE;
+}
+
 SpB_Info SpB_VNEC_plan_info_ext(const void* plan, SpB_VNEC_info_ext* info) {
   clear_error();
   Plan* p = find_plan(plan);

@@ -262,6 +262,62 @@ bool Plan::run_host(const void* h_x, void* h_y) {
   return device_status(own_stream);
 }
 
+Plan::HostPipe::~HostPipe() {
+  for (cudaStream_t q : {in, comp, out})
+    if (q) cudaStreamSynchronize(q);
+  for (int i = 0; i < 2; ++i)
+    for (cudaEvent_t e : {x_ready[i], comp_done[i], out_done[i]})
+      if (e) cudaEventDestroy(e);
+  for (cudaStream_t q : {in, comp, out})
+    if (q) cudaStreamDestroy(q);
+}
+
+bool Plan::HostPipe::init(size_t xb, size_t yb) {
+  for (cudaStream_t* q : {&in, &comp, &out})
+    if (!VNEC_CUDA(cudaStreamCreateWithFlags(q, cudaStreamNonBlocking))) return false;
+  for (int i = 0; i < 2; ++i) {
+    for (cudaEvent_t* e : {&x_ready[i], &comp_done[i], &out_done[i]})
+      if (!VNEC_CUDA(cudaEventCreateWithFlags(e, cudaEventDisableTiming))) return false;
+    if (!x[i].alloc(xb) || !y[i].alloc(yb)) return false;
+  }
+  return true;
+}
+
+bool Plan::run_host_async(const void* h_x, void* h_y) {
+  std::lock_guard<std::mutex> g(host_mu);
+  const size_t vb = type == SpB_FP64 ? 8 : 4;
+  const size_t nx = (size_t)n_cols * rhs, ny = (size_t)n_rows * rhs;
+  if (!pipe) {
+    auto p = std::make_unique<HostPipe>();
+    if (!p->init(vb * std::max<size_t>(nx, 1), vb * std::max<size_t>(ny, 1))) return false;
+    pipe = std::move(p);
+  }
+  HostPipe& q = *pipe;
+  const int s = (int)(q.calls & 1);
+  // Slot s was last used two calls ago: its x is free once that SpMV is done,
+  // its y once that copy-out is done.
+  if (q.used[s] && !VNEC_CUDA(cudaStreamWaitEvent(q.in, q.comp_done[s], 0))) return false;
+  if (nx > 0 && !VNEC_CUDA(cudaMemcpyAsync(q.x[s].ptr, h_x, vb * nx, cudaMemcpyHostToDevice, q.in))) return false;
+  if (!VNEC_CUDA(cudaEventRecord(q.x_ready[s], q.in)) || !VNEC_CUDA(cudaStreamWaitEvent(q.comp, q.x_ready[s], 0)))
+    return false;
+  if (q.used[s] && !VNEC_CUDA(cudaStreamWaitEvent(q.comp, q.out_done[s], 0))) return false;
+  if (!run_slot(s, q.x[s].ptr, q.y[s].ptr, q.comp) || !VNEC_CUDA(cudaEventRecord(q.comp_done[s], q.comp)) ||
+      !VNEC_CUDA(cudaStreamWaitEvent(q.out, q.comp_done[s], 0)))
+    return false;
+  if (ny > 0 && !VNEC_CUDA(cudaMemcpyAsync(h_y, q.y[s].ptr, vb * ny, cudaMemcpyDeviceToHost, q.out))) return false;
+  if (!VNEC_CUDA(cudaEventRecord(q.out_done[s], q.out))) return false;
+  q.used[s] = true;
+  ++q.calls;
+  return true;
+}
+
+bool Plan::host_wait() {
+  std::lock_guard<std::mutex> g(host_mu);
+  if (!pipe) return true;
+  if (!VNEC_CUDA(cudaStreamSynchronize(pipe->out)) || !VNEC_CUDA(cudaStreamSynchronize(pipe->in))) return false;
+  return device_status(pipe->comp);
+}
+
 namespace {
 std::mutex g_reg_mu;
 std::unordered_map<const void*, std::unique_ptr<Plan>>& registry() {
@@ -287,6 +343,10 @@ std::unique_ptr<Plan> take_plan(const void* handle) {
   if (it == registry().end()) return nullptr;
   std::unique_ptr<Plan> p = std::move(it->second);
   registry().erase(it);
+  // Pipelined host calls still in flight read the plan's device arrays.
+  if (p && p->pipe) {
+    for (cudaStream_t q : {p->pipe->in, p->pipe->comp, p->pipe->out}) cudaStreamSynchronize(q);
+  }
   return p;
 }
 

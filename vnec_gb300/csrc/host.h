@@ -94,6 +94,27 @@ struct Plan {
   // y := A x with host vectors: copy x in, SpMV, copy y out, synchronise.
   virtual bool run_host(const void* h_x, void* h_y);
   std::mutex host_mu;  // serialises host-vector calls (they share dx, dy and own_stream)
+  // Pipelined host-vector calls: enqueue returns at once; call i copies x in
+  // on one stream, computes on a second and copies y out on a third, using
+  // buffer slot i % 2, so call i+1's x copy and call i-1's y copy overlap
+  // call i's SpMV.  host_wait() waits for every enqueued call.
+  bool run_host_async(const void* h_x, void* h_y);
+  bool host_wait();
+  // The SpMV of one pipelined call (slot 0 or 1); default run().
+  virtual bool run_slot(int slot, const void* d_x, void* d_y, cudaStream_t s) {
+    (void)slot;
+    return run(d_x, d_y, s);
+  }
+  struct HostPipe {
+    cudaStream_t in = nullptr, comp = nullptr, out = nullptr;
+    DeviceBuffer x[2], y[2];
+    cudaEvent_t x_ready[2] = {nullptr, nullptr}, comp_done[2] = {nullptr, nullptr}, out_done[2] = {nullptr, nullptr};
+    bool used[2] = {false, false};
+    long long calls = 0;
+    bool init(size_t xb, size_t yb);
+    ~HostPipe();
+  };
+  std::unique_ptr<HostPipe> pipe;
 };
 
 // Registry: public handle pointer -> plan.
