@@ -56,6 +56,11 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "SpMV GB/s (% of GB300 HBM peak), mixed/batched vs plain FP64 at fixed rel. error"
+# --precision: sliced-kernel form of the main plan (api.PREC_*), its dtype label and error bound.
+PRECISIONS = {"fp64": 0, "fp32": 1, "bf16": 2, "df32": 3}
+PREC_DTYPE = {"fp64": "f64", "fp32": "f32 (fp64 reductions)", "bf16": "bf16 x row scale (fp32 products, fp64 reductions)",
+              "df32": "f32 hi+lo (double-float)"}
+PREC_TOL = {"fp64": 1e-12, "fp32": 1e-6, "bf16": 1e-2, "df32": 1e-12}
 L2_FLUSH_BYTES = 512 << 20
 
 
@@ -74,10 +79,11 @@ def workload(name: str):
         m = G.rmat(22, 1 << 26, 0.57, 0.19, 0.19, seed=1)
         x = G.vector(m.n_cols, lo=-1.0, hi=1.0, seed=1)
         desc = "rmat_scale22_edges2^26_a.57_b.19_c.19_dedup_fp64"
-    elif name == "stencil256":
-        m = G.stencil27(256, seed=0)
+    elif name in ("stencil256", "stencil128"):
+        g = int(name[len("stencil"):])
+        m = G.stencil27(g, seed=0)
         x = G.vector(m.n_cols, seed=0)
-        desc = "stencil27_256^3_fp64"
+        desc = f"stencil27_{g}^3_fp64"
     else:
         raise SystemExit(f"unknown workload {name}")
     return m, x, desc
@@ -341,7 +347,10 @@ def run_ours(args) -> None:
     t_plan = time.time()
     kernel = {"L": api.KERNEL_L, "S": api.KERNEL_S}[args.kernel]
     # Sliced plans time their unroll (4/8/12/16 loads in flight) on the matrix at build.
-    plan = api.Plan(m, kernel=kernel, items_per_thread=-1 if args.kernel == "S" else 0)
+    prec = PRECISIONS[args.precision]
+    if prec != api.PREC_FP64 and args.kernel != "S":
+        raise SystemExit("--precision applies to the sliced kernel (--kernel S)")
+    plan = api.Plan(m, kernel=kernel, items_per_thread=-1 if args.kernel == "S" else 0, precision=prec)
     t_plan = time.time() - t_plan
     info = plan.info()
     stream = torch.cuda.Stream(device=dev)
@@ -419,16 +428,21 @@ def run_ours(args) -> None:
     rel = O.rowwise_error(y_dev, y_ref, cond)
 
     peak, peak_src = measured_peaks()
-    kname = {"L": "mp2_kernel", "S": "sliced_kernel"}[args.kernel]
-    achieved = B / (np.mean(main_ms) / 1e3) / 1e9
-    traffic = profiled_traffic(kname, args.workload)
+    kname = {"L": "mp2_kernel", "S": "sliced_kernel" if prec == api.PREC_FP64 else "sliced_mixed_kernel"}[args.kernel]
+    # The kernel's own algorithmic bytes: stored value size of the form, 2-byte
+    # columns (plus a first column per row) where 16-bit deltas are used.
+    B_form = info.algorithmic_bytes if args.kernel == "S" else B
+    achieved = B_form / (np.mean(main_ms) / 1e3) / 1e9
+    traffic = profiled_traffic(kname, args.workload + ("" if prec == api.PREC_FP64 else "_" + args.precision))
     line = {
         "metric": METRIC, "value": round(value, 3), "unit": "GB/s", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(total_ms / args.steps, 5), "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "scaling": "weak", "vs_baseline": None, "dtype": PREC_DTYPE[args.precision],
         "data": "synthetic (seeded generator, resident in HBM before timing)",
-        "config": {"workload": desc, "n_rows": m.n_rows, "n_cols": m.n_cols, "nnz": m.nnz,
-                   "algorithmic_bytes": B,
+        "config": {"workload": desc + ("" if prec == api.PREC_FP64 else f"_{args.precision}_form"),
+                   "n_rows": m.n_rows, "n_cols": m.n_cols, "nnz": m.nnz,
+                   "algorithmic_bytes": B, "form_bytes": B_form,
+                   "value_bytes": "plain FP64 bytes (value and e2e are time ratios across forms)",
                    "kernel": {"L": "merge-path CSR (VNEC-L counterpart)",
                               "S": "sliced row groups (VNEC-S counterpart)"}[args.kernel],
                    "arithmetic": "fp64 fma" if info.arithmetic != 2 else "df32 (double-float on FP32 pipe)",
@@ -445,14 +459,14 @@ def run_ours(args) -> None:
                 "path": "SpB_mxv_host_async_ext: independent calls on page-locked host x/y, each copying x in, "
                         "running the SpMV and copying y out, consecutive calls overlapping (copies in, compute, "
                         "copies out on three streams); wall clock from first enqueue to SpB_VNEC_host_wait_ext; "
-                        "the matrix (3.2 GB) exceeds L2",
+                        f"the plan's device arrays ({info.device_bytes / 1e9:.1f} GB) exceed L2",
                 "sync_value": round(e2e_value, 3), "sync_steps": e2e_steps,
                 "sync_path": "SpB_mxv_host_ext, one blocking call per step (H2D x, SpMV in row-window parts, "
                              "D2H y per part), L2 flushed before each call"},
         "gpu_launches": args.steps * info.launches_per_call,
         "clocks": clocks,
         "rel_error": {"max_rowwise": float(rel.max()), "median_rowwise": float(np.median(rel)),
-                      "criterion": "|y-yhat| <= 1e-12 * sum|a x| (compensated FP64 oracle)"},
+                      "criterion": f"|y-yhat| <= {PREC_TOL[args.precision]:g} * sum|a x| (compensated FP64 oracle)"},
     }
     if not args.no_legs:
         legs = {args.workload: form_legs(m, xv, B, flush, stream, args.leg_steps, args.warmup)}
@@ -690,12 +704,14 @@ def main() -> None:
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", default="rmat24",
-                    choices=["rmat24", "rmat22", "uniform64k", "stencil256", "batch512"])
+                    choices=["rmat24", "rmat22", "uniform64k", "stencil256", "stencil128", "batch512"])
     ap.add_argument("--rhs", default="1,4,8,16,32", help="batch512: right-hand-side counts")
     ap.add_argument("--batch-precision", default="fp64", help="batch512: fp64,fp32")
     ap.add_argument("--batch-mats", type=int, default=512)
     ap.add_argument("--batch-steps", type=int, default=10)
     ap.add_argument("--kernel", default="S", choices=["L", "S"])
+    ap.add_argument("--precision", default="fp64", choices=list(PRECISIONS),
+                    help="sliced-kernel form of the main plan (the headline is fp64)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-legs", action="store_true", help="skip the precision-form / tuner / batch legs")
     ap.add_argument("--no-batch-leg", action="store_true", help="skip the batched-form legs of the default run")

@@ -98,6 +98,7 @@ struct SlicedHostView {
   const int64_t* win_task;
   const int64_t* win_long;
   const int64_t* win_entry;
+  int64_t delta_nnz, delta_rows;  // nonzeros and rows stored with 16-bit column deltas
 };
 SlicedHostView sliced_view(const SlicedHost* h);
 

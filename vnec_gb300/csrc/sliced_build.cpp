@@ -25,6 +25,7 @@ namespace vnec {
 
 struct SlicedHost {
   int64_t entries = 0, n_rowid = 0, num_long = 0, num_chunks = 0;
+  int64_t delta_nnz = 0, delta_rows = 0;  // nonzeros and rows stored with 16-bit column deltas
   int vpe = 1;
   std::vector<int64_t> win_task, win_long, win_entry;  // per-window offsets (windows + 1)
   std::vector<SlicedTask> tasks;
@@ -168,6 +169,7 @@ SlicedHost* sliced_build(int64_t n_rows, int64_t n_cols, const int64_t* rp, cons
   }
 
   // Pass 2: global task list and the interleaved entries.
+  std::vector<int64_t> win_dnnz((size_t)nwin, 0), win_drows((size_t)nwin, 0);
 #pragma omp parallel for schedule(dynamic, 1)
   for (int64_t w = 0; w < nwin; ++w) {
     Window& wd = win[(size_t)w];
@@ -227,7 +229,9 @@ SlicedHost* sliced_build(int64_t n_rows, int64_t n_cols, const int64_t* rp, cons
             const int64_t b = begin(r), len = begin(r + 1) - b;
             h->first[(size_t)(t.row_base + g)] = colat(b);
             for (int64_t j = 1; j < len; ++j) ddst[j * 32 + g] = (uint16_t)(colat(b + j) - colat(b + j - 1));
+            win_dnnz[(size_t)w] += len;
           }
+          win_drows[(size_t)w] += nrows;
           h->tasks[(size_t)(off_t[w] + (int64_t)ti)].meta |= kSlicedDelta;
         }
       } else {  // chunk of a long row
@@ -247,6 +251,10 @@ SlicedHost* sliced_build(int64_t n_rows, int64_t n_cols, const int64_t* rp, cons
     }
   }
   h->long_first[(size_t)h->num_long] = (int32_t)h->num_chunks;
+  for (int64_t w = 0; w < nwin; ++w) {
+    h->delta_nnz += win_dnnz[(size_t)w];
+    h->delta_rows += win_drows[(size_t)w];
+  }
   return h;
 }
 
@@ -272,6 +280,8 @@ SlicedHostView sliced_view(const SlicedHost* h) {
   v.win_task = h->win_task.data();
   v.win_long = h->win_long.data();
   v.win_entry = h->win_entry.data();
+  v.delta_nnz = h->delta_nnz;
+  v.delta_rows = h->delta_rows;
   return v;
 }
 

@@ -20,6 +20,7 @@ struct SlicedPlan final : Plan {
   std::vector<int32_t> hot_host;  // hot-column window: original column of each slot
   SlicedParams prm;
   int64_t blocks = 0;  // dense-block plans: number of blocks of 4
+  int64_t delta_nnz = 0, delta_rows = 0;  // stored with 16-bit column deltas (+ a first column per row)
   // Host-vector calls are split into parts (consecutive row windows) so that
   // the copy of one part's y rows to the host overlaps the next part's SpMV.
   struct Part {
@@ -168,7 +169,9 @@ struct SlicedPlan final : Plan {
     const int64_t io = type == SpB_FP64 ? 8 : 4;
     const int64_t sv = mx.precision == kPrecFP32 ? 4 : mx.precision == kPrecBF16 ? 2 : io;
     const int64_t scale = mx.precision == kPrecBF16 ? n_rows : 0;
-    return nnz * (sv + 4) + (n_rows + 1) * 4 + scale + n_cols * io + n_rows * io;
+    // Columns: 4 bytes, or 2 bytes per delta-coded nonzero plus its row's first column.
+    const int64_t cols = 4 * (nnz - delta_nnz) + 2 * delta_nnz + 4 * delta_rows;
+    return nnz * sv + cols + (n_rows + 1) * 4 + scale + n_cols * io + n_rows * io;
   }
   void describe(SpB_VNEC_info_ext* info) const override {
     info->kernel = kind == PlanKind::kWindowDense ? SpB_VNEC_KERNEL_D : SpB_VNEC_KERNEL_S;
@@ -406,6 +409,8 @@ std::unique_ptr<Plan> upload(std::unique_ptr<SlicedPlan> p, SlicedHost* h, int v
   m.long_first = p->long_first.as<int32_t>();
   m.chunk_sum = p->chunk_sum.ptr;
   m.lane_run = run;
+  p->delta_nnz = hv.col16 ? hv.delta_nnz : 0;
+  p->delta_rows = hv.col16 ? hv.delta_rows : 0;
   // Options: cache_hints 2 explicit L1/L2 policies, 3 no L1 allocation for the
   // streamed arrays, 4 the same with L1 evict-last x gathers; items_per_thread
   // selects the unroll (4, 8, 12, 16; default 12, the fastest of the four on
