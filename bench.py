@@ -24,7 +24,8 @@ reference protocol 1 warm-up + up to 40 calls), `clocks` (nvidia-smi sampled
 during the timed region), `rel_error` (against the compensated FP64 oracle),
 `legs` (per matrix — the headline matrix and, for R-MAT 2^24, the 256^3
 27-point stencil — the plain FP64 sliced kernel, its FP32 / BF16+row-scale /
-FP32 hi+lo forms and the learned and rule-based kernel selections: median ms
+FP32 hi+lo forms, the learned and rule-based kernel selections and the learned
+selection of the FP32 form (the mixed-precision, learned-tuned plan): median ms
 over --leg-steps flushed calls, speed-up over plain FP64, row-wise error),
 `batch_legs` (the batched form on 512 uneven matrices, k = 1 and 32, FP64 /
 FP32 / DF32, autotuned, 5 graph-replayed steps each).
@@ -261,7 +262,8 @@ def form_legs(m, xv, B: int, flush, stream, steps: int, warmup: int) -> dict:
     forms = [("fp64", S), ("fp32", dict(S, precision=api.PREC_FP32)),
              ("bf16_rowscale", dict(S, precision=api.PREC_BF16)),
              ("df32_hilo", dict(S, precision=api.PREC_DF32)),
-             ("learned", dict(kernel=api.KERNEL_LEARNED)), ("rule", dict(kernel=api.KERNEL_RULE))]
+             ("learned", dict(kernel=api.KERNEL_LEARNED)), ("rule", dict(kernel=api.KERNEL_RULE)),
+             ("learned_fp32", dict(kernel=api.KERNEL_LEARNED, precision=api.PREC_FP32))]
     base = None
     for name, kw in forms:
         t0 = time.time()
@@ -273,7 +275,7 @@ def form_legs(m, xv, B: int, flush, stream, steps: int, warmup: int) -> dict:
                "unroll": plan.info().items_per_thread,
                "max_rel_error": float(rel.max()), "median_rel_error": float(np.median(rel)),
                "plan_build_s": round(build_s, 2)}
-        if name in ("learned", "rule"):
+        if name in ("learned", "rule", "learned_fp32"):
             cfg, how = api.plan_choice(plan)
             leg["config"] = api.tune_configs()[cfg]
             leg["how"] = ["direct", "learned", "search", "rule", "fallback-search"][how]

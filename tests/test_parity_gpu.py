@@ -667,6 +667,31 @@ def test_precision_forms_error_bounds(built, prec):
         p.free()
 
 
+@pytest.mark.parametrize("kernel", ["LEARNED", "SEARCH", "AUTO"])
+def test_tuned_precision_forms(built, kernel):
+    """The learned / searched selection with a precision form chooses among the
+    pure sliced configurations (the plans that carry the forms) and keeps the
+    form's error bound; kernels without the forms refuse it."""
+    from vnec_gb300 import api
+    from vnec_gb300 import generators as G
+
+    cfgs = api.tune_configs()
+    kern = {"LEARNED": api.KERNEL_LEARNED, "SEARCH": api.KERNEL_SEARCH, "AUTO": api.KERNEL_AUTO}[kernel]
+    for m in (G.lognormal(40000, sigma=1.5, cap=3000, seed=4), G.stencil27(24, seed=5)):
+        xv = G.vector(m.n_cols, seed=6)
+        for prec in (api.PREC_FP32, api.PREC_BF16):
+            p = api.Plan(m, kernel=kern, precision=prec)
+            cfg, _ = api.plan_choice(p)
+            assert cfgs[cfg][0] != api.KERNEL_L and cfgs[cfg][2] > 1000, cfgs[cfg]  # pure sliced
+            assert p.info().precision == prec
+            check_f64(p.mxv_host(xv), m, xv, tol=PREC_TOL[prec])
+            p.free()
+    m = G.uniform_k(2000, 6, seed=1)
+    for k in (api.KERNEL_L, api.KERNEL_D, api.KERNEL_HYBRID, api.KERNEL_RULE):
+        with pytest.raises(api.VnecError):
+            api.Plan(m, kernel=k, precision=api.PREC_FP32)
+
+
 def test_bf16_row_scale_handles_wide_row_magnitudes(built):
     """Rows of very different magnitude: the power-of-two row scale keeps each
     row's relative error at BF16 precision."""

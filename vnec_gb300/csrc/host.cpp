@@ -436,6 +436,10 @@ bool values_df32_safe(const CsrView& v) {
 
 std::unique_ptr<Plan> build_merge_path(const CsrView& v, const SpB_VNEC_options_ext* opts) {
   if (!validate_csr(v, false)) return nullptr;
+  if (opts && opts->precision != 0) {
+    set_error("precision forms apply to sliced plans (kernel S, or LEARNED / SEARCH / AUTO)");
+    return nullptr;
+  }
   auto p = std::make_unique<MergePathPlan>();
   p->type = v.type;
   p->n_rows = v.n_rows;

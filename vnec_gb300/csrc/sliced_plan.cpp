@@ -534,6 +534,10 @@ std::unique_ptr<Plan> build_sliced(const CsrView& v, const SpB_VNEC_options_ext*
 // the sliced warp-task format.
 std::unique_ptr<Plan> build_dense(const CsrView& v, const SpB_VNEC_options_ext* opts, const uint8_t* keep) {
   if (!validate_csr(v, true)) return nullptr;
+  if (opts && opts->precision != 0) {
+    set_error("precision forms apply to sliced plans (kernel S, or LEARNED / SEARCH / AUTO)");
+    return nullptr;
+  }
   constexpr int W = 4;
   auto p = std::make_unique<SlicedPlan>(PlanKind::kWindowDense);
   p->type = v.type;
@@ -639,6 +643,10 @@ struct HybridPlan final : Plan {
 
 std::unique_ptr<Plan> build_hybrid(const CsrView& v, const SpB_VNEC_options_ext* opts) {
   if (!validate_csr(v, true)) return nullptr;
+  if (opts && opts->precision != 0) {
+    set_error("precision forms apply to sliced plans (kernel S, or LEARNED / SEARCH / AUTO)");
+    return nullptr;
+  }
   constexpr int W = 4;
   auto p = std::make_unique<HybridPlan>();
   p->type = v.type;

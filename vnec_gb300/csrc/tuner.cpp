@@ -38,8 +38,11 @@ bool cols_sorted(const CsrView& v) {
   return !bad;
 }
 
-bool available(int i, const CsrView& v, bool sorted) {
+// `precision`: a precision form of the sliced kernel restricts the choice to
+// the pure sliced configurations (the only plans that carry the forms).
+bool available(int i, const CsrView& v, bool sorted, int precision = 0) {
   const TuneConfig& c = kConfigs[i];
+  if (precision != 0) return c.kernel != SpB_VNEC_KERNEL_L && c.permille > 1000;
   if (c.kernel == SpB_VNEC_KERNEL_L) return c.chunk != 12 || v.type == SpB_FP64;
   // Rows in dense blocks need sorted columns; the pure-sliced configuration does not.
   return sorted || c.permille > 1000;
@@ -134,7 +137,7 @@ int autotune_search(const CsrView& v, const SpB_VNEC_options_ext* base, int reps
   }
   for (int i = 0; i < kNumConfigs; ++i) {
     ms[i] = FLT_MAX;
-    if (!available(i, v, sorted)) continue;
+    if (!available(i, v, sorted, base ? base->precision : 0)) continue;
     std::unique_ptr<Plan> p = build_config(i, v, base);
     if (!p) continue;
     ms[i] = time_plan(p.get(), dx.ptr, dy.ptr, flush.ptr, flush_bytes, reps, ts.s, ts.e0, ts.e1);
@@ -159,7 +162,7 @@ int rule_choice(const CsrView& v) {
 // Learned choice: the configuration with the lowest predicted cost among the
 // available ones; *ood is set when a feature lies outside the training range
 // (widened by 0.05 on each side).  Returns -1 when no model is built in.
-int learned_choice(const CsrView& v, bool* ood, float* pred) {
+int learned_choice(const CsrView& v, bool* ood, float* pred, int precision = 0) {
   float f[kNumFeatures];
   *ood = false;
   if (!builtin_mlp_params()) return -1;
@@ -177,7 +180,7 @@ int learned_choice(const CsrView& v, bool* ood, float* pred) {
   const bool sorted = cols_sorted(v);
   int best = -1;
   for (int i = 0; i < kNumConfigs; ++i)
-    if (available(i, v, sorted) && (best < 0 || out[i] < out[best])) best = i;
+    if (available(i, v, sorted, precision) && (best < 0 || out[i] < out[best])) best = i;
   return best;
 }
 
@@ -186,12 +189,17 @@ std::unique_ptr<Plan> build_tuned(const CsrView& v, const SpB_VNEC_options_ext* 
   if (!validate_csr(v, false)) return nullptr;
   const int kernel = opts ? opts->kernel : SpB_VNEC_KERNEL_LEARNED;
   int choice = -1, how = 0;
+  const int precision = opts ? opts->precision : 0;
   if (kernel == SpB_VNEC_KERNEL_RULE) {
+    if (precision != 0) {
+      set_error("the reference rule chooses among FP64 kernels: ask LEARNED or SEARCH for a precision form");
+      return nullptr;
+    }
     choice = rule_choice(v);
     how = SpB_VNEC_CHOSEN_RULE;
   } else if (kernel == SpB_VNEC_KERNEL_LEARNED) {
     bool ood = false;
-    choice = learned_choice(v, &ood, nullptr);
+    choice = learned_choice(v, &ood, nullptr, precision);
     how = SpB_VNEC_CHOSEN_LEARNED;
     if (choice < 0 || ood) choice = -1;
   }
