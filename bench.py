@@ -570,7 +570,9 @@ def batch_legs(mats, ks, precs, steps: int, warmup: int, dev, flush, stream, ws:
             for _ in range(e2e_steps):
                 plan.mxv_host(hx.numpy(), hy.numpy())
             e2e_s = time.perf_counter() - t0
-            pipe_steps = max(4, steps // 4)
+            # Enough calls that filling and draining the three-stage pipeline
+            # (one x copy in, one y copy out) does not dominate the rate.
+            pipe_steps = max(16, steps // 4)
             pipe_s, hy_pipe = pipelined_e2e(plan, hx.numpy(), n_rows * k, pipe_steps)
             y_dev = y.cpu().numpy()
             if not np.array_equal(hy.numpy(), y_dev) or not np.array_equal(hy_pipe, y_dev):
