@@ -162,6 +162,13 @@ typedef struct {
                             consecutive steps, read as 16-byte vectors (0: where most
                             entries use 16-bit column deltas, 1: on, -1: off; the sums
                             are the same either way) */
+  int hot_order;         /* sliced plans with a hot-column window: 0 (default) stores each
+                            row's hot-window entries first, hottest first, and groups rows
+                            of equal length by their hottest column, so the lanes of one
+                            gather step share x lines (the row sums change order: FP64
+                            results agree to rounding); -1 keeps CSR order within rows
+                            (bit-identical to the plan without a window) */
+  int reserved[7];
 } SpB_VNEC_options_ext;
 
 /* Precision forms of the sliced kernel for an FP64 matrix (x and y stay

@@ -339,8 +339,10 @@ HOT_SIZES = [1, 100, 4096, 1 << 20]
 
 @pytest.mark.parametrize("prec", [0, 1, 2, 3], ids=["fp64", "fp32", "bf16_rowscale", "df32_hilo"])
 def test_sliced_hot_column_window(built, prec):
-    """The hot-column window only relabels where x is read: every window size
-    gives the same bits as no window, for every precision form."""
+    """The hot-column window relabels where x is read: with CSR entry order
+    kept (hot_order -1) every window size gives the same bits as no window, for
+    every precision form; the default hot-first order (hottest entries first,
+    rows grouped by hottest column) changes only the summation order."""
     from vnec_gb300 import api
     from vnec_gb300 import generators as G
 
@@ -353,11 +355,13 @@ def test_sliced_hot_column_window(built, prec):
         p0.free()
         check_f64(y0, m, xv, tol=tol)
         for h in HOT_SIZES:
-            p = api.Plan(m, kernel=api.KERNEL_S, precision=prec, hot_columns=h, long_row_len=64)
-            y = p.mxv_host(xv)
-            check_f64(y, m, xv, tol=tol)
-            p.free()
-            p = api.Plan(m, kernel=api.KERNEL_S, precision=prec, hot_columns=h)
+            for kw in (dict(long_row_len=64), dict(), dict(window_rows=1000, max_steps=4)):
+                p = api.Plan(m, kernel=api.KERNEL_S, precision=prec, hot_columns=h, **kw)
+                y = p.mxv_host(xv)
+                check_f64(y, m, xv, tol=tol)
+                assert p.mxv_host(xv).tobytes() == y.tobytes()  # deterministic
+                p.free()
+            p = api.Plan(m, kernel=api.KERNEL_S, precision=prec, hot_columns=h, hot_order=-1)
             assert p.mxv_host(xv).tobytes() == y0.tobytes(), h
             p.free()
 

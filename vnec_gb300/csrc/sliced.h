@@ -66,6 +66,9 @@ struct SlicedParams {
   int max_steps = 32;         // target load steps per lane for grouped rows
   int hot = 0;                // hot-column window size (0: none)
   bool delta16 = false;       // 16-bit column deltas for VW = 1 groups whose rows allow it
+  // Optional secondary key of the row sort (rows of equal length in a window
+  // are grouped in ascending key order), n_rows values, or null.
+  const int32_t* row_key = nullptr;
 };
 
 // Host-side arrays of a built sliced matrix.

@@ -87,8 +87,11 @@ SlicedHost* sliced_build(int64_t n_rows, int64_t n_cols, const int64_t* rp, cons
       else
         longr.push_back((int32_t)r);
     }
-    std::stable_sort(grouped.begin(), grouped.end(),
-                     [&](int32_t a, int32_t b) { return begin(a + 1) - begin(a) < begin(b + 1) - begin(b); });
+    std::stable_sort(grouped.begin(), grouped.end(), [&](int32_t a, int32_t b) {
+      const int64_t la = begin(a + 1) - begin(a), lb = begin(b + 1) - begin(b);
+      if (la != lb) return la < lb;
+      return prm.row_key && prm.row_key[a] < prm.row_key[b];
+    });
     for (size_t i = 0; i < zero.size(); i += 32) {
       const int n = (int)std::min<size_t>(32, zero.size() - i);
       wd.tasks.push_back(SlicedTask{0, (int32_t)wd.rowid.size(), 0, meta(kSlicedZero, 0, n)});

@@ -2,6 +2,7 @@
 // dense-block format built on the same warp-task layout (VNEC-D counterpart).
 
 #include <algorithm>
+#include <climits>
 #include <cmath>
 #include <cstring>
 #include <limits>
@@ -220,6 +221,46 @@ bool choose_hot(const CsrView& v, int64_t want, double min_cover, std::vector<in
   }
   *hot = std::move(cand);
   return true;
+}
+
+// Hot-first entry order: within each row, the entries of hot-window columns
+// come first, hottest slot first, then the other entries in CSR order; `col`
+// (the relabelled columns) and the values are permuted in place of a copy.
+// row_key[r] is the slot of row r's first entry (n_cols + slot > n_cols for a
+// hot column, INT32_MAX otherwise): rows of equal length sorted by it put
+// rows sharing their hottest column side by side, so the lanes of one gather
+// step read the same few x lines.
+void hot_first_order(const CsrView& v, int32_t n_cols, const void* val, int vb, std::vector<int32_t>* col,
+                     std::vector<unsigned char>* out_val, std::vector<int32_t>* row_key) {
+  out_val->resize((size_t)std::max<int64_t>(v.nnz, 1) * vb);
+  row_key->assign((size_t)std::max<int64_t>(v.n_rows, 1), INT32_MAX);
+  const unsigned char* src = static_cast<const unsigned char*>(val);
+#pragma omp parallel
+  {
+    std::vector<int64_t> idx;
+    std::vector<int32_t> c;
+#pragma omp for schedule(dynamic, 4096)
+    for (int64_t r = 0; r < v.n_rows; ++r) {
+      const int64_t b = v.row_begin(r), e = v.row_begin(r + 1);
+      if (e == b) continue;
+      idx.resize((size_t)(e - b));
+      for (int64_t q = b; q < e; ++q) idx[(size_t)(q - b)] = q;
+      // Hot entries (relabelled >= n_cols) by slot, then the rest in CSR order.
+      std::stable_sort(idx.begin(), idx.end(), [&](int64_t a, int64_t bq) {
+        const int32_t ca = (*col)[(size_t)a], cb = (*col)[(size_t)bq];
+        const bool ha = ca >= n_cols, hb = cb >= n_cols;
+        if (ha != hb) return ha;
+        return ha && ca < cb;
+      });
+      c.resize(idx.size());
+      for (size_t k = 0; k < idx.size(); ++k) {
+        c[k] = (*col)[(size_t)idx[k]];
+        std::memcpy(out_val->data() + (size_t)(b + (int64_t)k) * vb, src + (size_t)idx[k] * vb, (size_t)vb);
+      }
+      std::copy(c.begin(), c.end(), col->begin() + b);
+      if (c[0] >= n_cols) (*row_key)[(size_t)r] = c[0];
+    }
+  }
 }
 
 // Window size asked for by the options (0: none) and the coverage it needs.
@@ -504,7 +545,8 @@ std::unique_ptr<Plan> build_sliced(const CsrView& v, const SpB_VNEC_options_ext*
     }
     src_val = scaled.data();
   }
-  std::vector<int32_t> mapped;
+  std::vector<int32_t> mapped, row_key;
+  std::vector<unsigned char> ordered_val;
   const int32_t* cols = v.idx;
   const uint64_t* cols64 = v.idx64;
   double min_cover = 0.0;
@@ -513,6 +555,11 @@ std::unique_ptr<Plan> build_sliced(const CsrView& v, const SpB_VNEC_options_ext*
     cols = mapped.data();
     cols64 = nullptr;
     p->prm.hot = (int)p->hot_host.size();
+    if (!(opts && opts->hot_order < 0)) {
+      hot_first_order(v, (int32_t)v.n_cols, src_val, vb, &mapped, &ordered_val, &row_key);
+      src_val = ordered_val.data();
+      p->prm.row_key = row_key.data();
+    }
   }
   // 16-bit column deltas where rows allow them (not with a hot window, whose
   // relabelled columns break the increasing order).
