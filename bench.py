@@ -197,14 +197,27 @@ def reference_cores_and_parts() -> tuple[int, int, str]:
 
 
 def cpu_time_L(m, x, warm: int, reps: int, budget_s: float) -> tuple[float, int, str]:
-    """Seconds per call of the reference's VNEC-L FP64 on the host (oracle port)."""
+    """Seconds per call of the reference's own dispatch on the host (oracle port):
+    VNEC-L FP64 for n >= 3e6 rows (test_spmv_vnec.cpp:197), else VNEC-S FP64
+    (IRD_VNEC picks S for the sparse configurations timed here)."""
     from oracle import oracle as O
 
     cores, nparts, arch = reference_cores_and_parts()
-    t1 = O.time_L_f64(m, x, nparts, warm=warm, reps=1)
+    build = dict(O.ARM if arch in ("aarch64", "arm64") else O.X86, nparts=nparts)
+    if m.n_rows >= 3_000_000:
+        name = "VNEC-L"
+
+        def run(w, r):
+            return O.time_L_f64(m, x, nparts, warm=w, reps=r)
+    else:
+        name = f"VNEC-S (IRD {O.ird(m, build=build)[1]:.3f})"
+
+        def run(w, r):
+            return O.time_S_f64(m, x, build=build, warm=w, reps=r)
+    t1 = run(warm, 1)
     reps = int(max(1, min(reps, budget_s / max(t1, 1e-9))))
-    secs = O.time_L_f64(m, x, nparts, warm=0, reps=reps)
-    return secs, reps, f"VNEC-L FP64 restated (oracle port), {nparts} OpenMP partitions/threads on {cores} {arch} cores"
+    secs = run(0, reps)
+    return secs, reps, f"{name} FP64 restated (oracle port), {nparts} OpenMP partitions/threads on {cores} {arch} cores"
 
 
 def time_plan_device(plan, x, y, flush, stream, steps: int, warmup: int) -> list[float]:
@@ -310,13 +323,11 @@ def run_reference(args) -> None:
         return
     m, x, desc = workload(args.workload)
     B = algorithmic_bytes(m)
-    cores, nparts, arch = reference_cores_and_parts()
-    from oracle import oracle as O
-
-    per_call = O.time_L_f64(m, x, nparts, warm=args.warmup, reps=args.steps)
+    cores, _, _ = reference_cores_and_parts()
+    per_call, reps, how = cpu_time_L(m, x, warm=args.warmup, reps=args.steps, budget_s=max(args.cpu_budget, 60.0))
     value = B / per_call / 1e9
-    sample = (f"full workload, {args.warmup} warm-up + {args.steps} timed SpMV_VNEC_L_FP64 calls (the reference "
-              f"dispatch for n >= 3e6), restated in C (oracle port); {nparts} OpenMP threads on {cores} {arch} cores")
+    sample = (f"full workload, {args.warmup} warm-up + {reps} timed calls of the reference harness's dispatch "
+              f"(L for n >= 3e6, else IRD's choice): {how}")
     line = {"impl": "reference", "metric": METRIC, "value": round(value, 3), "unit": "GB/s", "n_gpus": ws,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(per_call * 1e3, 4),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
@@ -381,7 +392,8 @@ def run_ours(args) -> None:
     w0 = time.time()
     with torch.cuda.stream(stream):
         for k in range(args.steps):
-            flush.fill_(k)
+            if args.l2 == "flushed":
+                flush.fill_(k)
             starts[k].record(stream)
             plan.mxv_device(x.data_ptr(), y.data_ptr(), stream.cuda_stream)
             ends[k].record(stream)
@@ -449,7 +461,8 @@ def run_ours(args) -> None:
                               "S": "sliced row groups (VNEC-S counterpart)"}[args.kernel],
                    "arithmetic": "fp64 fma" if info.arithmetic != 2 else "df32 (double-float on FP32 pipe)",
                    "tile": f"{info.threads_per_block}x{info.items_per_thread}", "tiles": info.num_tiles,
-                   "l2": "flushed before every timed step (512 MiB device write, outside the events)",
+                   "l2": ("flushed before every timed step (512 MiB device write, outside the events)"
+                          if args.l2 == "flushed" else "warm: no flush between steps (inputs may stay in L2)"),
                    "parallelism": "replicas" if ws > 1 else "single GPU",
                    "gen_s": round(t_gen, 2), "plan_build_s": round(t_plan, 2)},
         "roofline": {"bound": "hbm", "kernel": kname, "achieved": round(achieved, 1), "peak": peak,
@@ -714,6 +727,8 @@ def main() -> None:
     ap.add_argument("--batch-mats", type=int, default=512)
     ap.add_argument("--batch-steps", type=int, default=10)
     ap.add_argument("--kernel", default="S", choices=["L", "S"])
+    ap.add_argument("--l2", default="flushed", choices=["flushed", "warm"],
+                    help="flush L2 before each timed step (default) or keep it warm (small workloads' warm figure)")
     ap.add_argument("--precision", default="fp64", choices=list(PRECISIONS),
                     help="sliced-kernel form of the main plan (the headline is fp64)")
     ap.add_argument("--no-cpu-baseline", action="store_true")

@@ -58,6 +58,8 @@ def lib() -> C.CDLL:
         L.orc_partition.argtypes = [C.c_int, _i64, _i64, _vp, _vp, _vp, _vp, _vp]
         L.orc_time_L_f64.argtypes = [C.c_int, _i64, _i64] + [_vp] * 5 + [C.c_int, C.c_int]
         L.orc_time_L_f64.restype = C.c_double
+        L.orc_time_S_f64.argtypes = [C.c_int, C.c_int, _i64, _i64, _i64] + [_vp] * 5 + [C.c_int, C.c_int]
+        L.orc_time_S_f64.restype = C.c_double
         L.orc_num_procs.restype = C.c_int
         _lib = L
     return _lib
@@ -164,6 +166,16 @@ def time_L_f64(m, x, nparts: int, warm: int = 1, reps: int = 40) -> float:
     xx = np.ascontiguousarray(x, dtype=np.float64)
     y = np.zeros(m.n_rows)
     return lib().orc_time_L_f64(nparts, m.n_rows, m.nnz, _p(rp), _p(ci), _p(v), _p(xx), _p(y), warm, reps)
+
+
+def time_S_f64(m, x, build=ARM, warm: int = 1, reps: int = 40) -> float:
+    """Seconds per SpMV_VNEC_S_FP64 call of the restatement (format built once)."""
+    rp, ci = _csr(m)
+    v = np.ascontiguousarray(m.val, dtype=np.float64)
+    xx = np.ascontiguousarray(x, dtype=np.float64)
+    y = np.zeros(m.n_rows)
+    return lib().orc_time_S_f64(build["nparts"], build["nlanes_f64"], m.n_rows, m.n_cols, m.nnz, _p(rp), _p(ci),
+                                _p(v), _p(xx), _p(y), warm, reps)
 
 
 def ref_spmv(variant: int, m, x, dtype=np.float64) -> tuple[np.ndarray, int, float]:

@@ -635,13 +635,19 @@ static void s_free(orc_s_t *s) {
  * in-row rows (AVX512_spvv_in_row_fp64 :127-152 / NEON :277-301) use nlanes lane
  * accumulators while i < rowlen - (nlanes - 1), sum = 0 + reduction, then a
  * scalar fma tail.  No carry: partitions hold whole rows. */
-void orc_spmv_S_f64(int nparts, int nlanes, i64 n_rows, i64 n_cols, i64 nnz, const i64 *row_ptr,
-                    const int32_t *col, const double *val, const double *x, double *y, int reps) {
+/* `warm` untimed then `reps` timed calls after one build (the reference times
+ * only SpMV_VNEC_S_FP64, test_spmv_vnec.cpp:205-214); seconds per timed call. */
+static double s_run_f64(int nparts, int nlanes, i64 n_rows, i64 n_cols, i64 nnz, const i64 *row_ptr,
+                        const int32_t *col, const double *val, const double *x, double *y, int warm, int reps) {
   orc_s_t s;
   s_build(&s, nparts, nlanes, n_rows, n_cols, nnz, row_ptr, col, val, NULL);
   double **win = malloc(sizeof(double *) * nparts);
   for (int t = 0; t < nparts; ++t) win[t] = calloc((size_t)s.e.nec[t] + 1, sizeof(double));
-  for (int rep = 0; rep < reps; ++rep) {
+  double t0 = 0.0;
+  for (int rep = 0; rep < warm + reps; ++rep) {
+#ifdef _OPENMP
+    if (rep == warm) t0 = omp_get_wtime();
+#endif
 #pragma omp parallel for schedule(static) num_threads(nparts)
     for (int t = 0; t < nparts; ++t) {
       double *w = win[t];
@@ -670,9 +676,25 @@ void orc_spmv_S_f64(int nparts, int nlanes, i64 n_rows, i64 n_cols, i64 nnz, con
       }
     }
   }
+  double secs = 0.0;
+#ifdef _OPENMP
+  secs = (omp_get_wtime() - t0) / (reps > 0 ? reps : 1);
+#endif
   for (int t = 0; t < nparts; ++t) free(win[t]);
   free(win);
   s_free(&s);
+  return secs;
+}
+
+void orc_spmv_S_f64(int nparts, int nlanes, i64 n_rows, i64 n_cols, i64 nnz, const i64 *row_ptr,
+                    const int32_t *col, const double *val, const double *x, double *y, int reps) {
+  s_run_f64(nparts, nlanes, n_rows, n_cols, nnz, row_ptr, col, val, x, y, 0, reps);
+}
+
+/* Timed S-variant loop for the CPU baseline; seconds per call. */
+double orc_time_S_f64(int nparts, int nlanes, i64 n_rows, i64 n_cols, i64 nnz, const i64 *row_ptr,
+                      const int32_t *col, const double *val, const double *x, double *y, int warm, int reps) {
+  return s_run_f64(nparts, nlanes, n_rows, n_cols, nnz, row_ptr, col, val, x, y, warm, reps);
 }
 
 /* SpMV_VNEC_S_FP32, spmv_vnec_S_for_mxv.c:255-334 with the FP32 micro-kernels

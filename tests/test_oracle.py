@@ -131,3 +131,20 @@ def test_oracle_matches_live_reference_on_fresh_matrices(built):
             for var, code in (("D", 1), ("S", 2), ("L", 3)):
                 y_ref, _, _ = O.ref_spmv(code, m, x, dtype=dt)
                 assert carry_equal(O.spmv_vnec(var, m, x, dtype=dt), y_ref, m, x), (var, dt)
+
+
+def test_timed_cpu_baseline_loops(built):
+    """The timed loops behind the CPU baseline (VNEC-L and VNEC-S FP64, format
+    built once, `reps` calls) compute the same y as the untimed restatement and
+    return a positive time per call."""
+    from oracle import oracle as O
+    from vnec_gb300 import generators as G
+
+    m = G.uniform_k(4096, 16, seed=0)
+    x = G.vector(m.n_cols, seed=1)
+    for build in (O.X86, O.ARM):
+        assert O.time_S_f64(m, x, build=build, warm=1, reps=3) > 0.0
+        assert O.time_L_f64(m, x, build["nparts"], warm=1, reps=3) > 0.0
+    y_ref, cond = O.spmv_neumaier(m, x)
+    y = O.spmv_vnec("S", m, x, build=O.ARM)
+    assert np.all(np.abs(y - y_ref) <= 1e-12 * cond)
