@@ -418,7 +418,8 @@ def test_sliced_column_deltas(built, prec):
         xv = G.vector(m.n_cols, seed=8)
         ys = []
         for cd in (-1, 0):
-            p = api.Plan(m, kernel=api.KERNEL_S, precision=prec, column_deltas=cd, hot_columns=-1)
+            # max_steps 32: one row per lane for these rows, the groups that can hold deltas
+            p = api.Plan(m, kernel=api.KERNEL_S, precision=prec, column_deltas=cd, hot_columns=-1, max_steps=32)
             ys.append(p.mxv_host(xv))
             p.free()
         assert ys[0].tobytes() == ys[1].tobytes()
@@ -438,6 +439,7 @@ def test_sliced_lane_vectors(built, kw):
 
     kw = dict(kw)
     u = kw.pop("unroll", 12)
+    kw.setdefault("max_steps", 32)  # one row per lane (delta groups) at these sizes
     for m in (G.stencil27(20, seed=3), G.banded(20000, 13, seed=2), G.lognormal(20000, sigma=1.3, cap=900, seed=5),
               G.rmat(14, 1 << 18, seed=6), _edge_matrix("hub_rows_and_empties")):
         xv = G.vector(m.n_cols, seed=8)
