@@ -524,7 +524,7 @@ def batch_bytes(nnz: int, n_rows: int, n_cols: int, n_mats: int, k: int, vb: int
     return nnz * (vb + 4) + (n_rows + n_mats) * 4 + (n_rows + n_cols) * k * 8
 
 
-def batch_legs(mats, ks, precs, steps: int, warmup: int, dev, flush, stream, ws: int = 1):
+def batch_legs(mats, ks, precs, steps: int, warmup: int, dev, flush, stream, ws: int = 1, tile=None):
     """Every (precision, k) of the batched form on `mats`: autotuned plan, graph
     replays timed with CUDA events (L2 flushed before each), end-to-end host
     calls and error on every 32nd matrix.  Returns (legs, launches, first leg)."""
@@ -544,7 +544,11 @@ def batch_legs(mats, ks, precs, steps: int, warmup: int, dev, flush, stream, ws:
     for prec in precs:
         for k in ks:
             t_plan = time.time()
-            plan = api.BatchPlan(mats, k, precision=prec, autotune=True)
+            if tile:  # fixed layout (lanes, long-row limit, warps per block, unroll), no autotune
+                plan = api.BatchPlan(mats, k, precision=prec, lanes=tile[0], long_row_len=tile[1],
+                                     warps_per_block=tile[2], unroll=tile[3])
+            else:
+                plan = api.BatchPlan(mats, k, precision=prec, autotune=True)
             t_plan = time.time() - t_plan
             info = plan.info()
             ro, co = plan.offsets()
@@ -655,7 +659,9 @@ def run_batch(args) -> None:
     peak, peak_src = measured_peaks()
     sampler = ClockSampler(dev.index)
     w0 = time.time()
-    legs, gpu_launches, first = batch_legs(mats, ks, precs, args.batch_steps, args.warmup, dev, flush, stream, ws)
+    tile = [int(v) for v in args.batch_tile.split(",")] if args.batch_tile else None
+    legs, gpu_launches, first = batch_legs(mats, ks, precs, args.batch_steps, args.warmup, dev, flush, stream, ws,
+                                           tile=tile)
     w1 = time.time()
     clocks = sampler.stop(w0, w1)
     leg, B = first
@@ -726,6 +732,8 @@ def main() -> None:
     ap.add_argument("--batch-precision", default="fp64", help="batch512: fp64,fp32")
     ap.add_argument("--batch-mats", type=int, default=512)
     ap.add_argument("--batch-steps", type=int, default=10)
+    ap.add_argument("--batch-tile", default="", help="batch512: fixed lanes,long_row_len,warps_per_block,unroll "
+                                                     "instead of the autotuner")
     ap.add_argument("--kernel", default="S", choices=["L", "S"])
     ap.add_argument("--l2", default="flushed", choices=["flushed", "warm"],
                     help="flush L2 before each timed step (default) or keep it warm (small workloads' warm figure)")

@@ -373,7 +373,9 @@ typedef struct {
   int no_graph;        /* 1: launch the kernels directly on each call */
   int window_rows;     /* rows sorted by length within windows of this size (0: 65536) */
   int max_steps;       /* a row group spreads over enough slots to take at most this many steps (0: 32) */
-  int unroll;          /* load steps in flight per lane: 1 normal, 2 doubled; 0: tuned or normal */
+  int unroll;          /* kernel mode: 1 normal load steps in flight per lane, 2 doubled, 3 each
+                          task's columns and values read in bulk (128 per round) and passed to
+                          the slots by shuffles; 0: tuned or normal */
   int host_parts;      /* host-vector calls run in this many parts so that X and Y copies overlap the
                           compute (0: 8, 1: one part) */
   int reserved[5];
@@ -394,7 +396,7 @@ void *SpB_VNEC_batch_plan_matrices_ext(int n_mats, const SpB_Matrix *A, int k,
 SpB_Info SpB_VNEC_batch_offsets_ext(const void *plan, int64_t *row_offset, int64_t *col_offset);
 
 /* Autotuner result of a batch plan: candidates timed (0 if not tuned) and,
- * per candidate, {lanes, long_row_len, warps_per_block, doubled unroll 0/1}
+ * per candidate, {lanes, long_row_len, warps_per_block, kernel mode 0/1/2 (unroll - 1)}
  * and its median milliseconds on the sample (up to `cap` entries); *best =
  * chosen index. */
 int SpB_VNEC_batch_tuning_ext(const void *plan, int *configs, float *ms, int cap, int *best);

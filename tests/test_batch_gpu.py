@@ -93,7 +93,7 @@ def test_batch_all_lanes(built, batch, k, precision):
     chunked rows (and the in-kernel long-row completion) are exercised."""
     from vnec_gb300 import api
 
-    for L, unroll in [(L, u) for L in lanes_for(k) for u in (1, 2)]:
+    for L, unroll in [(L, u) for L in lanes_for(k) for u in (1, 2, 3)]:
         p = api.BatchPlan(batch, k, lanes=L, long_row_len=64, precision=precision, max_steps=4, unroll=unroll)
         try:
             ro, co = p.offsets()
@@ -106,6 +106,26 @@ def test_batch_all_lanes(built, batch, k, precision):
                 check(Y, Yref, cond, TOL[precision])
         finally:
             p.free()
+
+
+@pytest.mark.parametrize("k", [1, 4, 8, 32])
+@pytest.mark.parametrize("precision", [0, 1, 3], ids=["fp64", "fp32", "df32"])
+def test_batch_staged_entries_bit_identical(built, batch, k, precision):
+    """Kernel mode 3 (each task's columns and values read in bulk and passed to
+    the slots by shuffles) sums the same steps in the same order as mode 1:
+    identical Y for every lanes layout, with long rows spanning several bulk
+    rounds."""
+    from vnec_gb300 import api
+
+    for L in lanes_for(k):
+        ys = []
+        for unroll in (1, 3):
+            p = api.BatchPlan(batch, k, lanes=L, long_row_len=2048, precision=precision, unroll=unroll)
+            try:
+                ys.append(p.mxv_host(_x(p, k)))
+            finally:
+                p.free()
+        assert ys[0].tobytes() == ys[1].tobytes(), L
 
 
 @pytest.mark.parametrize("k", [1, 8, 32])
@@ -237,7 +257,7 @@ def test_batch_autotune(built, batch, precision):
     p = api.BatchPlan(batch, k, autotune=True, precision=precision)
     try:
         cand, ms, best = p.tuning()
-        assert len(cand) == len(lanes_for(k)) * 3 * 2 * 2
+        assert len(cand) == len(lanes_for(k)) * 3 * 2 * 3  # lanes x long-row limit x warps x kernel mode
         assert 0 <= best < len(cand) and all(t > 0 for t in ms)
         assert ms[best] == min(ms)
         inf = p.info()

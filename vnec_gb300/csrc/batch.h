@@ -36,7 +36,7 @@ struct BatchMatrix {
   int* chunk_count = nullptr;           // num_long arrival counters, 0 between calls
   int grid = 0;                         // persistent CTAs
   int warps_per_block = 8;
-  bool deep = false;                    // twice the load steps in flight per lane
+  int mode = 0;                         // 0: U steps in flight, 1: 2U, 2: entries staged in registers
   int precision = 0;                    // kPrecFP64, kPrecFP32 or kPrecDF32 (SlicedPrecision)
   void* xbuf = nullptr;                 // FP32 / DF32: n_cols * k converted X
   int* flag = nullptr;                  // DF32: X outside the split range this call
@@ -73,8 +73,8 @@ BatchHostView batch_view(const BatchHost* h);
 
 // k in {1, 2, 4, ..., 32}, lanes a divisor of 32 with k / lanes in {1, 2, 4, 8}.
 bool batch_supported(int k, int lanes);
-// Persistent CTAs for the kernel of (precision, k / lanes, warps_per_block, deep unroll).
-int batch_grid(int precision, int rhs_per_lane, int warps_per_block, bool deep);
+// Persistent CTAs for the kernel of (precision, k / lanes, warps_per_block, mode).
+int batch_grid(int precision, int rhs_per_lane, int warps_per_block, int mode);
 // Y = A X for the whole batch: one persistent kernel (the FP32 form first
 // rounds X into xbuf).  Long rows are finished inside the kernel by the last
 // of their chunks to arrive.

@@ -156,7 +156,20 @@ struct CodecDF32Guard {
   __device__ static double out(const A& a) { return a.s; }
 };
 
-template <class Cd, int R, int U>
+__device__ __forceinline__ double shfl_val(double v, int src) { return __shfl_sync(kFull, v, src); }
+__device__ __forceinline__ float shfl_val(float v, int src) { return __shfl_sync(kFull, v, src); }
+__device__ __forceinline__ float2 shfl_val(float2 v, int src) {
+  return make_float2(__shfl_sync(kFull, v.x, src), __shfl_sync(kFull, v.y, src));
+}
+
+// STAGED: each task's (column, value) entries are read 32 * kStageRounds at a
+// time with one coalesced load per lane per 32 entries, and every step's pair
+// reaches its slot's lanes by shuffles, so inside the step loop only the X
+// gathers wait on memory.  Otherwise every step's pair is loaded by the slot's
+// lanes (broadcast), U steps in flight.
+constexpr int kStageRounds = 4;
+
+template <class Cd, int R, int U, bool STAGED = false>
 __device__ __forceinline__ void run_tasks(const BatchArgs& a, const typename Cd::X* __restrict__ x) {
   using V = typename Cd::V;
   using X = typename Cd::X;
@@ -182,6 +195,47 @@ __device__ __forceinline__ void run_tasks(const BatchArgs& a, const typename Cd:
 #pragma unroll
     for (int r = 0; r < R; ++r) acc[r] = Cd::zero();
     int s = 0;
+    if constexpr (STAGED) {
+      const int E = steps * S;  // entries of the task
+      const int spr = 32 / S;   // steps per 32 entries (= L)
+      const int32_t* cb = a.col + base;
+      const V* vb = val + base;
+      for (int e0 = 0; e0 < E; e0 += 32 * kStageRounds) {
+        int creg[kStageRounds];
+        V vreg[kStageRounds];
+#pragma unroll
+        for (int b = 0; b < kStageRounds; ++b) {
+          const int e = e0 + b * 32 + lane;
+          creg[b] = e < E ? __ldcs(cb + e) : 0;
+          vreg[b] = e < E ? __ldcs(vb + e) : V{};
+        }
+#pragma unroll
+        for (int b = 0; b < kStageRounds; ++b) {
+          const int sb = (e0 + b * 32) / S;  // first step held by register round b
+          if (sb >= steps) break;
+          for (int j = 0; j < spr; j += U) {
+            int c[U];
+            V v[U];
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+              const int src = (((j + u) * S) & 31) + slot;
+              c[u] = __shfl_sync(kFull, creg[b], src);
+              v[u] = shfl_val(vreg[b], src);
+            }
+            X xv[U][R];
+#pragma unroll
+            for (int u = 0; u < U; ++u)
+              if (j + u < spr && sb + j + u < steps) load_vec<X, R>(xs + ((size_t)c[u] << a.klog2), xv[u]);
+#pragma unroll
+            for (int u = 0; u < U; ++u)
+              if (j + u < spr && sb + j + u < steps)
+#pragma unroll
+                for (int r = 0; r < R; ++r) Cd::mac(acc[r], v[u], xv[u][r]);
+          }
+        }
+      }
+      s = steps;
+    }
     for (; s + U <= steps; s += U) {
       int c[U];
       V v[U];
@@ -251,37 +305,43 @@ __device__ __forceinline__ void run_tasks(const BatchArgs& a, const typename Cd:
   }
 }
 
-template <class Cd, int R, int U>
+template <class Cd, int R, int U, bool STAGED>
 __global__ void __launch_bounds__(256) batch_kernel(const BatchArgs a) {
-  run_tasks<Cd, R, U>(a, static_cast<const typename Cd::X*>(a.x));
+  run_tasks<Cd, R, U, STAGED>(a, static_cast<const typename Cd::X*>(a.x));
 }
 
-template <int R, int U>
+template <int R, int U, bool STAGED>
 __global__ void __launch_bounds__(256) batch_df32_kernel(const BatchArgs a) {
   if (*reinterpret_cast<const volatile int*>(a.flag))
-    run_tasks<CodecDF32Guard, R, U>(a, a.x64);
+    run_tasks<CodecDF32Guard, R, U, STAGED>(a, a.x64);
   else
-    run_tasks<CodecDF32, R, U>(a, static_cast<const float2*>(a.x));
+    run_tasks<CodecDF32, R, U, STAGED>(a, static_cast<const float2*>(a.x));
 }
 
-// Steps in flight per lane: 8 / R (at least 2), doubled with `deep`.
-template <int R, bool DEEP> constexpr int unroll_for() { return (R >= 4 ? 2 : 8 / R) * (DEEP ? 2 : 1); }
+// Steps in flight per lane: 8 / R (at least 2), doubled in mode 1; mode 2
+// stages the entries in registers (STAGED) with the mode-0 step count.
+template <int R, int MODE> constexpr int unroll_for() { return (R >= 4 ? 2 : 8 / R) * (MODE == 1 ? 2 : 1); }
 
-template <int R, bool DEEP> void* kernel_for(int precision) {
-  constexpr int U = unroll_for<R, DEEP>();
+template <int R, int MODE> void* kernel_for(int precision) {
+  constexpr int U = unroll_for<R, MODE>();
+  constexpr bool ST = MODE == 2;
   switch (precision) {
-    case kPrecFP32: return reinterpret_cast<void*>(&batch_kernel<CodecF32, R, U>);
-    case kPrecDF32: return reinterpret_cast<void*>(&batch_df32_kernel<R, U>);
-    default: return reinterpret_cast<void*>(&batch_kernel<CodecF64, R, U>);
+    case kPrecFP32: return reinterpret_cast<void*>(&batch_kernel<CodecF32, R, U, ST>);
+    case kPrecDF32: return reinterpret_cast<void*>(&batch_df32_kernel<R, U, ST>);
+    default: return reinterpret_cast<void*>(&batch_kernel<CodecF64, R, U, ST>);
   }
 }
 
-void* pick_kernel(int precision, int r, bool deep) {
+template <int R> void* kernel_for_mode(int precision, int mode) {
+  return mode == 2 ? kernel_for<R, 2>(precision) : mode == 1 ? kernel_for<R, 1>(precision) : kernel_for<R, 0>(precision);
+}
+
+void* pick_kernel(int precision, int r, int mode) {
   switch (r) {
-    case 1: return deep ? kernel_for<1, true>(precision) : kernel_for<1, false>(precision);
-    case 2: return deep ? kernel_for<2, true>(precision) : kernel_for<2, false>(precision);
-    case 4: return deep ? kernel_for<4, true>(precision) : kernel_for<4, false>(precision);
-    case 8: return deep ? kernel_for<8, true>(precision) : kernel_for<8, false>(precision);
+    case 1: return kernel_for_mode<1>(precision, mode);
+    case 2: return kernel_for_mode<2>(precision, mode);
+    case 4: return kernel_for_mode<4>(precision, mode);
+    case 8: return kernel_for_mode<8>(precision, mode);
     default: return nullptr;
   }
 }
@@ -294,8 +354,8 @@ int log2i(int v) {
 
 }  // namespace
 
-int batch_grid(int precision, int rhs_per_lane, int warps_per_block, bool deep) {
-  void* fn = pick_kernel(precision, rhs_per_lane, deep);
+int batch_grid(int precision, int rhs_per_lane, int warps_per_block, int mode) {
+  void* fn = pick_kernel(precision, rhs_per_lane, mode);
   if (!fn || (warps_per_block != 4 && warps_per_block != 8)) return 0;
   int dev = 0, sms = 0, per_sm = 0;
   if (!VNEC_CUDA(cudaGetDevice(&dev)) ||
@@ -344,7 +404,7 @@ bool batch_spmm_range(const BatchMatrix& m, const double* X, double* Y, cudaStre
   a.y = Y;
   a.klog2 = log2i(m.k);
   a.llog2 = log2i(m.lanes);
-  void* fn = pick_kernel(m.precision, R, m.deep);
+  void* fn = pick_kernel(m.precision, R, m.mode);
   const int grid = (int)std::min<long long>(m.grid, std::max<long long>(1, (a.num_tasks + 7) / 8));
   void* args[] = {&a};
   return VNEC_CUDA(cudaLaunchKernel(fn, dim3((unsigned)grid), dim3((unsigned)(m.warps_per_block * 32)), args, 0, s));

@@ -43,7 +43,7 @@ bool up(DeviceBuffer& b, const void* src, size_t bytes, size_t extra = 64) {
   return bytes == 0 || VNEC_CUDA(cudaMemcpy(b.ptr, src, bytes, cudaMemcpyHostToDevice));
 }
 
-bool upload_batch(const BatchHost* h, int k, int precision, int wpb, bool deep, BatchDev* d) {
+bool upload_batch(const BatchHost* h, int k, int precision, int wpb, int mode, BatchDev* d) {
   const BatchHostView v = batch_view(h);
   const size_t ne = (size_t)v.entries + 64;
   if (!up(d->tasks, v.tasks, sizeof(SlicedTask) * (size_t)v.num_tasks) ||
@@ -94,8 +94,8 @@ bool upload_batch(const BatchHost* h, int k, int precision, int wpb, bool deep, 
   m.xbuf = d->xbuf.ptr;
   m.precision = precision;
   m.warps_per_block = wpb;
-  m.deep = deep;
-  m.grid = batch_grid(precision, k / v.lanes, wpb, deep);
+  m.mode = mode;
+  m.grid = batch_grid(precision, k / v.lanes, wpb, mode);
   if (m.grid <= 0) {
     set_error("batch: no occupancy for the kernel");
     return false;
@@ -163,7 +163,7 @@ BatchHost* build_host(const BatchSource& s, const std::vector<int>& pick, int k,
 
 struct TuneChoice {
   int lanes = 0, long_len = 1024, wpb = 8;
-  int deep = 0;  // 1: twice the load steps in flight per lane
+  int deep = 0;  // kernel mode: 1 twice the load steps in flight, 2 entries staged in registers
 };
 
 std::mutex g_tune_mu;
@@ -276,7 +276,7 @@ float median_ms(std::vector<float> v) {
 }
 
 bool autotune(const BatchSource& s, int k, int precision, const SpB_VNEC_batch_options_ext* o, TuneRun* run) {
-  std::vector<int> lanes_c, long_c{256, 1024, 4096}, wpb_c{4, 8}, deep_c{0, 1};
+  std::vector<int> lanes_c, long_c{256, 1024, 4096}, wpb_c{4, 8}, deep_c{0, 1, 2};
   for (int L = 1; L <= 32; L <<= 1)
     if (batch_supported(k, L)) lanes_c.push_back(L);
   if (o->lanes > 0) lanes_c = {o->lanes};
@@ -319,8 +319,8 @@ bool autotune(const BatchSource& s, int k, int precision, const SpB_VNEC_batch_o
         }
         for (int deep : deep_c) {
           // The unroll changes only the kernel: same layout, new grid.
-          d.m.deep = deep != 0;
-          d.m.grid = batch_grid(precision, k / L, wpb, d.m.deep);
+          d.m.mode = deep;
+          d.m.grid = batch_grid(precision, k / L, wpb, d.m.mode);
           std::vector<float> t;
           for (int rep = 0; rep < 7 && ok; ++rep) {
             ok = VNEC_CUDA(cudaEventRecord(e0, st)) && batch_spmm(d.m, X.as<double>(), Y.as<double>(), st) &&
@@ -562,7 +562,7 @@ std::unique_ptr<Plan> build_batch(int n, const CsrView* mats, int k, const SpB_V
     set_error("batch: warps_per_block must be 4 or 8");
     return nullptr;
   }
-  if (o.long_row_len < 0 || o.chunk < 0 || o.window_rows < 0 || o.max_steps < 0 || o.unroll < 0 || o.unroll > 2) {
+  if (o.long_row_len < 0 || o.chunk < 0 || o.window_rows < 0 || o.max_steps < 0 || o.unroll < 0 || o.unroll > 3) {
     set_error("batch: negative option");
     return nullptr;
   }
@@ -650,7 +650,7 @@ std::unique_ptr<Plan> build_batch(int n, const CsrView* mats, int k, const SpB_V
     set_error("batch: more than 2^31 rows, columns or layout entries");
     return nullptr;
   }
-  const bool ok = upload_batch(h, k, o.precision, choice.wpb, choice.deep != 0, &p->d);
+  const bool ok = upload_batch(h, k, o.precision, choice.wpb, choice.deep, &p->d);
   if (ok) plan_parts(p.get(), batch_view(h), o.host_parts > 0 ? o.host_parts : 8);
   batch_free(h);
   if (!ok) return nullptr;
