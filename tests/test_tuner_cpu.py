@@ -89,5 +89,8 @@ def test_committed_dataset_is_consistent():
     assert fin.any(axis=1).all()
     best = np.argmin(np.where(fin, d["ms"], np.inf), axis=1)
     assert np.array_equal(best, d["best"])
-    assert set(np.unique(d["family"])) == set(range(len(DS.FAMILIES)))
-    assert d["n_rows"].min() >= 1e4 and d["n_rows"].max() <= 4.2e6
+    small = d["seed"] < DS.LARGE_FIRST
+    assert set(np.unique(d["family"][small])) == set(range(5))
+    assert d["n_rows"][small].min() >= 1e4 and d["n_rows"][small].max() <= 4.2e6
+    if (~small).any():  # large records: 4e6 - 1.7e7 rows
+        assert d["n_rows"][~small].min() >= 3.9e6 and d["n_rows"][~small].max() <= 1.7e7

@@ -4,7 +4,9 @@ Seeded synthetic FP64 matrices from a generator mix — uniform random, R-MAT
 (a in [0.45, 0.65]), banded (bandwidth 3-257), block-diagonal with dense
 8x8-64x64 blocks and lognormal row lengths (sigma in [0.5, 3]) — with row
 counts log-uniform in [1e4, 4e6] (reduced where a matrix would exceed
-MAX_NNZ nonzeros).  Each record holds the 16 features (GPU feature kernel),
+MAX_NNZ nonzeros), and large records (seeds from LARGE_FIRST: 4e6 - 1.7e7
+rows, R-MAT up to scale 24, 27-point stencils up to 256^3).  Each record
+holds the 16 features (GPU feature kernel),
 the exhaustive autotuner's median time of every configuration on this GPU,
 the reference rule's choice and the algorithmic bytes of one SpMV.
 
@@ -21,19 +23,60 @@ import numpy as np
 from .. import api
 from .. import generators as G
 
-FAMILIES = ("uniform", "rmat", "banded", "blockdiag", "lognormal")
+FAMILIES = ("uniform", "rmat", "banded", "blockdiag", "lognormal", "stencil")
 MAX_NNZ = 60_000_000
 ROWS_LO, ROWS_HI = 1e4, 4e6
+# Records with seed >= LARGE_FIRST: large matrices (4e6 - 1.7e7 rows, up to
+# LARGE_MAX_NNZ nonzeros: R-MAT scale 22-24, 27-point stencils, uniform,
+# banded, lognormal), so that workloads of the headline size lie inside the
+# trained feature range.
+LARGE_FIRST = 3000
+LARGE_MAX_NNZ = 300_000_000
+LARGE_ROWS_LO, LARGE_ROWS_HI = 4e6, 1.7e7
 
 
 def _loguni(rng, lo, hi):
     return math.exp(rng.uniform(math.log(lo), math.log(hi)))
 
 
+def sample_large(seed: int):
+    rng = np.random.default_rng([seed, 0x1A26E])
+    fam = ("rmat", "stencil", "uniform", "banded", "lognormal")[seed % 5]
+    n = int(_loguni(rng, LARGE_ROWS_LO, LARGE_ROWS_HI))
+    gseed = 1000 + seed
+    if fam == "rmat":
+        a = rng.uniform(0.5, 0.6)
+        b = c = (0.95 - a) / 2
+        scale = 22 + (seed // 5) % 3  # 22, 23, 24 in turn
+        deg = rng.uniform(8, 17)
+        m = G.rmat(scale, int(min(LARGE_MAX_NNZ, deg * (1 << scale))), a, b, c, lo=0.0, hi=1.0, seed=gseed)
+        desc = f"rmat scale={scale} a={a:.3f} deg={deg:.1f}"
+    elif fam == "stencil":
+        g = int(round(n ** (1.0 / 3.0)))
+        m = G.stencil27(g, seed=gseed)
+        desc = f"stencil27 g={g}"
+    elif fam == "uniform":
+        k = int(rng.integers(4, 25))
+        m = G.uniform_k(min(n, LARGE_MAX_NNZ // k), k, seed=gseed)
+        desc = f"uniform k={k}"
+    elif fam == "banded":
+        bw = int(round(_loguni(rng, 3, 63))) | 1
+        m = G.banded(min(n, LARGE_MAX_NNZ // bw), bw, seed=gseed)
+        desc = f"banded bw={bw}"
+    else:
+        sigma = rng.uniform(0.5, 1.5)
+        mean_len = 8.0 * math.exp(sigma * sigma / 2)
+        m = G.lognormal(int(min(n, LARGE_MAX_NNZ / mean_len)), sigma=sigma, cap=4096, seed=gseed)
+        desc = f"lognormal sigma={sigma:.2f}"
+    return m, fam, desc
+
+
 def sample(seed: int):
     """The matrix of record `seed` and a short description."""
+    if seed >= LARGE_FIRST:
+        return sample_large(seed)
     rng = np.random.default_rng([seed, 0x7E57])
-    fam = FAMILIES[seed % len(FAMILIES)]
+    fam = FAMILIES[seed % 5]
     n = int(_loguni(rng, ROWS_LO, ROWS_HI))
     gseed = 1000 + seed
     if fam == "uniform":

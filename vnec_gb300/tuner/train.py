@@ -6,7 +6,8 @@ T_CAP; configurations that cannot be built are masked out).  The MLP
 (16 -> 64 -> 64 -> C, FP32) is trained with Adam on masked squared error by
 the library's forward/backward/update kernels; its choice for a matrix is
 the configuration with the lowest predicted cost.  Records with seed < 2000
-train, seeds 2000-2199 are held out; regret = ms[choice] / ms[best] - 1.
+and three of every four large records train; seeds 2000-2199 and the other
+large records are held out; regret = ms[choice] / ms[best] - 1.
 
     python -m vnec_gb300.tuner.train --data shard*.npz --weights tuner_weights.inc --report report.json
 """
@@ -54,7 +55,11 @@ def summary(choice: np.ndarray, ms: np.ndarray, nbytes: np.ndarray) -> dict:
 
 
 def split(d: dict):
-    tr = d["seed"] < N_TRAIN
+    """(training, held-out) records: seeds below N_TRAIN and three of every four
+    large records train."""
+    s = d["seed"]
+    large = s >= dataset.LARGE_FIRST
+    tr = (s < N_TRAIN) | (large & ((s - dataset.LARGE_FIRST) % 4 != 3))
     return {k: v[tr] for k, v in d.items()}, {k: v[~tr] for k, v in d.items()}
 
 
