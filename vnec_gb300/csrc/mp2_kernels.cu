@@ -149,7 +149,7 @@ template <class M, int TPB, int IPT, int S>
 __global__ void __launch_bounds__(TPB) mp2_kernel(const Mp2Args a) {
   using L = Mp2Layout<TPB, IPT>;
   using Acc = typename M::Acc;
-  constexpr int kIPC = L::kIPC, kCap = L::kCap, kW = L::kWarps;
+  constexpr int kCap = L::kCap, kW = L::kWarps;
   extern __shared__ __align__(128) unsigned char smem[];
   unsigned char* const stage_base = smem;
   double* const xbuf = reinterpret_cast<double*>(smem + S * L::kStage);  // [2][kCap]

@@ -59,7 +59,7 @@ inline int meta(int kind, int vwl, int nrows) { return kind | (vwl << 4) | (nrow
 
 }  // namespace
 
-SlicedHost* sliced_build(int64_t n_rows, int64_t n_cols, const int64_t* rp, const uint64_t* rp64, const int32_t* ci,
+SlicedHost* sliced_build(int64_t n_rows, int64_t /*n_cols*/, const int64_t* rp, const uint64_t* rp64, const int32_t* ci,
                          const uint64_t* ci64, const void* val, int vb, const SlicedParams& prm, int vpe,
                          const uint8_t* keep) {
   // Each entry carries `vpe` consecutive values (1 for single nonzeros, the
