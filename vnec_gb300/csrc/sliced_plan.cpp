@@ -209,6 +209,11 @@ bool choose_hot(const CsrView& v, int64_t want, double min_cover, std::vector<in
   int64_t covered = 0;
   for (int32_t c : cand) covered += cnt[(size_t)c];
   if ((double)covered < min_cover * (double)v.nnz) return false;
+  // The default window also needs skew: its columns must carry at least 4x
+  // their share of the nonzeros (uniform column use gains nothing from a
+  // window but pays its gather launch).
+  if (min_cover > 0.0 && (double)covered * (double)v.n_cols < 4.0 * (double)cand.size() * (double)v.nnz)
+    return false;
   std::vector<int32_t> slot((size_t)v.n_cols, -1);
   for (size_t s = 0; s < cand.size(); ++s) slot[(size_t)cand[s]] = (int32_t)s;
   mapped->resize((size_t)v.nnz);
@@ -265,7 +270,8 @@ void hot_first_order(const CsrView& v, int32_t n_cols, const void* val, int vb, 
 
 // Window size asked for by the options (0: none) and the coverage it needs.
 // Default: 32,768 columns (the best of 4K-4M on R-MAT 2^24, FP64 and FP32
-// forms), built when they carry at least 5 % of the nonzeros.
+// forms), built when they carry at least 5 % of the nonzeros and at least 4x
+// their share of them.
 constexpr int64_t kHotDefault = 32768;
 constexpr double kHotMinCover = 0.05;
 int64_t hot_window(const SpB_VNEC_options_ext* opts, double* min_cover) {
