@@ -358,7 +358,7 @@ def run_ours(args) -> None:
     t_gen = time.time() - t_gen
     B = algorithmic_bytes(m)
     t_plan = time.time()
-    kernel = {"L": api.KERNEL_L, "S": api.KERNEL_S}[args.kernel]
+    kernel = {"L": api.KERNEL_L, "S": api.KERNEL_S, "D": api.KERNEL_D}[args.kernel]
     # Sliced plans time their unroll (4/8/12/16 loads in flight) on the matrix at build.
     prec = PRECISIONS[args.precision]
     if prec != api.PREC_FP64 and args.kernel != "S":
@@ -442,10 +442,11 @@ def run_ours(args) -> None:
     rel = O.rowwise_error(y_dev, y_ref, cond)
 
     peak, peak_src = measured_peaks()
-    kname = {"L": "mp2_kernel", "S": "sliced_kernel" if prec == api.PREC_FP64 else "sliced_mixed_kernel"}[args.kernel]
+    kname = {"L": "mp2_kernel", "D": "dense_block_kernel",
+             "S": "sliced_kernel" if prec == api.PREC_FP64 else "sliced_mixed_kernel"}[args.kernel]
     # The kernel's own algorithmic bytes: stored value size of the form, 2-byte
     # columns (plus a first column per row) where 16-bit deltas are used.
-    B_form = info.algorithmic_bytes if args.kernel == "S" else B
+    B_form = info.algorithmic_bytes if args.kernel in ("S", "D") else B
     achieved = B_form / (np.mean(main_ms) / 1e3) / 1e9
     traffic = profiled_traffic(kname, args.workload + ("" if prec == api.PREC_FP64 else "_" + args.precision))
     line = {
@@ -458,7 +459,8 @@ def run_ours(args) -> None:
                    "algorithmic_bytes": B, "form_bytes": B_form,
                    "value_bytes": "plain FP64 bytes (value and e2e are time ratios across forms)",
                    "kernel": {"L": "merge-path CSR (VNEC-L counterpart)",
-                              "S": "sliced row groups (VNEC-S counterpart)"}[args.kernel],
+                              "S": "sliced row groups (VNEC-S counterpart)",
+                              "D": "dense blocks of 4 columns (VNEC-D counterpart)"}[args.kernel],
                    "arithmetic": "fp64 fma" if info.arithmetic != 2 else "df32 (double-float on FP32 pipe)",
                    "tile": f"{info.threads_per_block}x{info.items_per_thread}", "tiles": info.num_tiles,
                    "l2": ("flushed before every timed step (512 MiB device write, outside the events)"
@@ -734,7 +736,7 @@ def main() -> None:
     ap.add_argument("--batch-steps", type=int, default=10)
     ap.add_argument("--batch-tile", default="", help="batch512: fixed lanes,long_row_len,warps_per_block,unroll "
                                                      "instead of the autotuner")
-    ap.add_argument("--kernel", default="S", choices=["L", "S"])
+    ap.add_argument("--kernel", default="S", choices=["L", "S", "D"])
     ap.add_argument("--l2", default="flushed", choices=["flushed", "warm"],
                     help="flush L2 before each timed step (default) or keep it warm (small workloads' warm figure)")
     ap.add_argument("--precision", default="fp64", choices=list(PRECISIONS),

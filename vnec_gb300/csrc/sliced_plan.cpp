@@ -170,6 +170,9 @@ struct SlicedPlan final : Plan {
     const int64_t io = type == SpB_FP64 ? 8 : 4;
     const int64_t sv = mx.precision == kPrecFP32 ? 4 : mx.precision == kPrecBF16 ? 2 : io;
     const int64_t scale = mx.precision == kPrecBF16 ? n_rows : 0;
+    // Dense-block plans move whole blocks: 4 values and one start column each.
+    if (kind == PlanKind::kWindowDense)
+      return blocks * (4 * sv + 4) + (n_rows + 1) * 4 + n_cols * io + n_rows * io;
     // Columns: 4 bytes, or 2 bytes per delta-coded nonzero plus its row's first column.
     const int64_t cols = 4 * (nnz - delta_nnz) + 2 * delta_nnz + 4 * delta_rows;
     return nnz * sv + cols + (n_rows + 1) * 4 + scale + n_cols * io + n_rows * io;
