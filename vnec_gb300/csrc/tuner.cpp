@@ -152,7 +152,8 @@ int autotune_search(const CsrView& v, const SpB_VNEC_options_ext* base, int reps
 // VNEC-S — here the merge path, the pure dense-block configuration and the
 // pure sliced configuration with their default chunk.
 int rule_choice(const CsrView& v) {
-  if (v.n_rows >= 3000000) return 1;
+  // VNEC-L: the merge-path configuration a default L plan takes at this size.
+  if (v.n_rows >= 3000000) return v.nnz >= ((int64_t)1 << 26) ? 0 : 1;
   const IrdParams prm = ird_params(v.type);
   const float ird = ird_ratio(v, prm);
   const bool dense = ird >= prm.threshold && cols_sorted(v);
