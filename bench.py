@@ -442,7 +442,7 @@ def run_ours(args) -> None:
     rel = O.rowwise_error(y_dev, y_ref, cond)
 
     peak, peak_src = measured_peaks()
-    kname = {"L": "mp2_kernel", "D": "dense_block_kernel",
+    kname = {"L": "mp2_kernel" if info.pipeline_stages else "mp_spmv_kernel", "D": "dense_block_kernel",
              "S": "sliced_kernel" if prec == api.PREC_FP64 else "sliced_mixed_kernel"}[args.kernel]
     # The kernel's own algorithmic bytes: stored value size of the form, 2-byte
     # columns (plus a first column per row) where 16-bit deltas are used.
