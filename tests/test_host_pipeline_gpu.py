@@ -82,3 +82,42 @@ def test_async_rejects_wrong_dtype(built):
         p.mxv_host_async(np.zeros(m.n_cols, dtype=np.float32), np.zeros(m.n_rows))
     p.host_wait()  # nothing enqueued
     p.free()
+
+
+@pytest.mark.parametrize("kind", ["S", "L", "HYBRID"])
+def test_host_calls_from_many_threads(built, kind):
+    """Host-vector calls on one plan from several host threads (ctypes releases
+    the GIL, so the calls overlap in the library): each thread's results equal
+    the single-threaded ones bit for bit."""
+    import threading
+
+    from vnec_gb300 import generators as G
+
+    m = G.lognormal(50000, sigma=1.3, cap=3000, seed=12)
+    p = _plan(kind, m)
+    xs = [G.vector(m.n_cols, seed=40 + i) for i in range(8)]
+    want = [p.mxv_host(x) for x in xs]
+    errors = []
+
+    def worker(t):
+        try:
+            for rep in range(6):
+                i = (t + rep) % len(xs)
+                if rep % 3 == 2:
+                    y = np.empty(m.n_rows)
+                    p.mxv_host_async(xs[i], y)
+                    p.host_wait()
+                else:
+                    y = p.mxv_host(xs[i])
+                if y.tobytes() != want[i].tobytes():
+                    errors.append((t, rep, i))
+        except Exception as e:  # noqa: BLE001 - reported below
+            errors.append((t, repr(e)))
+
+    threads = [threading.Thread(target=worker, args=(t,)) for t in range(4)]
+    for th in threads:
+        th.start()
+    for th in threads:
+        th.join()
+    p.free()
+    assert not errors, errors
