@@ -168,7 +168,9 @@ typedef struct {
                             gather step share x lines (the row sums change order: FP64
                             results agree to rounding); -1 keeps CSR order within rows
                             (bit-identical to the plan without a window) */
-  int reserved[7];
+  int offsets64;         /* merge-path plans: 1 stores row ends and merge coordinates as 64-bit
+                            integers (always done from 2^31 - 1 rows + nonzeros on) */
+  int reserved[6];
 } SpB_VNEC_options_ext;
 
 /* Precision forms of the sliced kernel for an FP64 matrix (x and y stay

@@ -131,6 +131,34 @@ def test_kernel_variants(built, label, kw):
         p.free()
 
 
+@pytest.mark.parametrize("dtype", [np.float64, np.float32], ids=["fp64", "fp32"])
+def test_merge_path_64bit_offsets(built, dtype):
+    """The 64-bit row-end / merge-coordinate variant (taken from 2^31 - 1 rows +
+    nonzeros on, forced here by offsets64) computes the same tiles as the
+    32-bit one: identical y, for every unpipelined tile shape and the edge
+    matrices."""
+    from vnec_gb300 import api
+    from vnec_gb300 import generators as G
+
+    mats = [G.rmat(15, 16 << 15, seed=4), G.lognormal(20000, sigma=2.5, cap=4096, seed=5),
+            _edge_matrix("single_row_spanning_tiles"), _edge_matrix("hub_rows_and_empties"),
+            _edge_matrix("all_rows_empty")]
+    for m in mats:
+        xv = np.random.default_rng(6).uniform(-1, 1, size=m.n_cols)
+        for t, i in UNPIPELINED:
+            ys = []
+            for o64 in (0, 1):
+                p = api.Plan(m, dtype=dtype, kernel=api.KERNEL_L, threads_per_block=t, items_per_thread=i,
+                             pipeline_stages=1, offsets64=o64)
+                ys.append(p.mxv_host(xv.astype(dtype)))
+                p.free()
+            assert ys[0].tobytes() == ys[1].tobytes(), (t, i)
+        if dtype == np.float64:
+            check_f64(ys[1], m, xv)
+        else:
+            check_f32(ys[1], m, xv)
+
+
 def test_df32_falls_back_to_fp64_for_out_of_range_x(built):
     """An x outside the double-float range raises the device flag; the guard
     launch recomputes the call in FP64, the next call is back on DF32."""

@@ -446,7 +446,7 @@ std::unique_ptr<Plan> build_merge_path(const CsrView& v, const SpB_VNEC_options_
   p->n_cols = v.n_cols;
   p->nnz = v.nnz;
   cudaGetDevice(&p->device);
-  const bool wide = (v.n_rows + v.nnz) >= ((int64_t)1 << 31) - 1;
+  const bool wide = (v.n_rows + v.nnz) >= ((int64_t)1 << 31) - 1 || (opts && opts->offsets64 > 0);
   const int req_stages = opts ? opts->pipeline_stages : 0;
   const int req_arith = opts ? opts->arithmetic : SpB_VNEC_ARITH_AUTO;
   // The pipelined kernel serves FP64 matrices with int32 merge coordinates.
