@@ -158,8 +158,8 @@ typedef struct {
   int column_deltas;     /* sliced: store the columns of one-row-per-lane groups as 16-bit
                             deltas where the gaps allow (0: on unless a hot-column window
                             is used, -1: off) */
-  int lane_vectors;      /* sliced FP32 form: each lane's entries stored in runs of 4
-                            consecutive steps, read as 16-byte vectors (0: where most
+  int lane_vectors;      /* sliced FP32 / BF16 forms: each lane's entries stored in runs of 4 /
+                            8 consecutive steps, read as 16-byte vectors (0: where most
                             entries use 16-bit column deltas, 1: on, -1: off; the sums
                             are the same either way) */
   int hot_order;         /* sliced plans with a hot-column window: 0 (default) stores each

@@ -458,10 +458,12 @@ def test_sliced_column_deltas(built, prec):
                                 dict(long_row_len=64, max_steps=7), dict(unroll=4), dict(unroll=8),
                                 dict(unroll=16)],
                          ids=["deltas", "cols", "hot", "chunks_odd_steps", "u4", "u8", "u16"])
-def test_sliced_lane_vectors(built, kw):
-    """FP32 lane runs (each lane's consecutive entries side by side, read as
-    16-byte vectors) change only the storage order: y is bit-identical to the
-    stride-32 layout, with whole runs, ragged tails, chunks and wide row groups."""
+@pytest.mark.parametrize("prec", [1, 2], ids=["fp32", "bf16_rowscale"])
+def test_sliced_lane_vectors(built, kw, prec):
+    """Lane runs (each lane's consecutive entries side by side, read as 16-byte
+    vectors: 4 FP32 or 8 BF16 steps) change only the storage order: y is
+    bit-identical to the stride-32 layout, with whole runs, ragged tails,
+    chunks and wide row groups."""
     from vnec_gb300 import api
     from vnec_gb300 import generators as G
 
@@ -473,11 +475,11 @@ def test_sliced_lane_vectors(built, kw):
         xv = G.vector(m.n_cols, seed=8)
         ys = []
         for lv in (-1, 1):
-            p = api.Plan(m, kernel=api.KERNEL_S, precision=1, lane_vectors=lv, items_per_thread=u, **kw)
+            p = api.Plan(m, kernel=api.KERNEL_S, precision=prec, lane_vectors=lv, items_per_thread=u, **kw)
             ys.append(p.mxv_host(xv))
             p.free()
         assert ys[0].tobytes() == ys[1].tobytes()
-        check_f64(ys[1], m, xv, tol=PREC_TOL[1])
+        check_f64(ys[1], m, xv, tol=PREC_TOL[prec])
 
 
 def test_sliced_full_size_rmat_scale24(built):

@@ -51,7 +51,7 @@ struct SlicedMatrix {
   bool hot_ready = false;             // xhot already gathered for this call (later parts of a split call)
   const uint16_t* col16 = nullptr;    // delta tasks (kSlicedDelta): 16-bit column deltas
   const int32_t* first = nullptr;     // delta tasks: first column of each row slot
-  // FP32 form: 0, or P when val / col / col16 hold each lane's entries
+  // FP32 / BF16 forms: 0, or P when val / col / col16 hold each lane's entries
   // in runs of P consecutive steps.  Steps [P*b, P*b + P) of a task's lane l
   // sit at base + b*32*P + l*P + (step - P*b), so a lane reads a run with one
   // 16-byte vector load; the last steps % P steps keep the stride-32 layout

@@ -245,13 +245,57 @@ sliced_mixed_kernel(const SlicedTask* __restrict__ tasks, long long num_tasks, c
   constexpr int UB = P > 0 ? 2 * U / P : 1;                  // runs per round
   constexpr int VW = P > 0 ? P * (int)sizeof(Val) / 4 : 1;  // words per value run
   constexpr int TL = P > 1 ? P - 1 : 1;                      // stride-32 steps after the runs
+  // BF16 runs (8 steps) instead take U / 4 runs at a time, then single runs,
+  // and sum the ragged tail in a final loop: fewer registers, more warps.
+  constexpr bool kSerialTail = sizeof(Val) == 2;
+  constexpr int UBS = U / 4 > 0 ? U / 4 : 1;
   if (meta & kSlicedDelta) {
     // One row per lane, columns as 16-bit deltas from the row's first column.
     const Val* vp = val + base + lane;
     const uint16_t* dp = col16 + base + lane;
     int c = lane < nrows ? __ldg(first + row_base + lane) : 0;
     typename C::Acc acc = C::zero();
-    if constexpr (P > 0) {
+    if constexpr (P > 0 && kSerialTail) {
+      constexpr int DW = P / 2;
+      const int nb = steps / P;
+      const Val* vr = val + base + lane * P;
+      const uint16_t* dr = col16 + base + lane * P;
+      int b = 0;
+      for (; b + UBS <= nb; b += UBS) {
+        uint32_t vw[UBS][VW], dw[UBS][DW];
+#pragma unroll
+        for (int u = 0; u < UBS; ++u) {
+          ld_words(dr + (b + u) * 32 * P, dw[u]);
+          ld_words(vr + (b + u) * 32 * P, vw[u]);
+        }
+#pragma unroll
+        for (int u = 0; u < UBS; ++u)
+#pragma unroll
+          for (int t = 0; t < P; ++t) {
+            c += run_at<uint16_t>(dw[u], t);
+            acc = C::mac(acc, run_at<Val>(vw[u], t), xs, c);
+          }
+      }
+      for (; b < nb; ++b) {
+        uint32_t vw[VW], dw[DW];
+        ld_words(dr + b * 32 * P, dw);
+        ld_words(vr + b * 32 * P, vw);
+#pragma unroll
+        for (int t = 0; t < P; ++t) {
+          c += run_at<uint16_t>(dw, t);
+          acc = C::mac(acc, run_at<Val>(vw, t), xs, c);
+        }
+      }
+      for (int k = nb * P; k < steps; ++k) {
+        c += __ldcs(dp + k * 32);
+        acc = C::mac(acc, ld_stream(vp + k * 32), xs, c);
+      }
+      if (lane < nrows) {
+        const double s = C::to_f64(acc);
+        y[rowid[row_base + lane]] = row_scale ? s * pow2(row_scale[row_base + lane]) : s;
+      }
+      return;
+    } else if constexpr (P > 0) {
       constexpr int DW = P / 2;  // words per delta run
       const int nb = steps / P, k0 = nb * P;
       const int row = lane < nrows ? __ldg(rowid + row_base + lane) : 0;
@@ -324,7 +368,32 @@ sliced_mixed_kernel(const SlicedTask* __restrict__ tasks, long long num_tasks, c
   const int32_t* cp = col + base + lane;
   typename C::Acc acc = C::zero();
   int k = 0;
-  if constexpr (P > 0) {
+  if constexpr (P > 0 && kSerialTail) {
+    const int nb = steps / P;
+    const Val* vr = val + base + lane * P;
+    const int32_t* cr = col + base + lane * P;
+    int b = 0;
+    for (; b + UBS <= nb; b += UBS) {
+      uint32_t vw[UBS][VW], cw[UBS][P];
+#pragma unroll
+      for (int u = 0; u < UBS; ++u) {
+        ld_words(cr + (b + u) * 32 * P, cw[u]);
+        ld_words(vr + (b + u) * 32 * P, vw[u]);
+      }
+#pragma unroll
+      for (int u = 0; u < UBS; ++u)
+#pragma unroll
+        for (int t = 0; t < P; ++t) acc = C::mac(acc, run_at<Val>(vw[u], t), xs, (int)cw[u][t]);
+    }
+    for (; b < nb; ++b) {
+      uint32_t vw[VW], cw[P];
+      ld_words(cr + b * 32 * P, cw);
+      ld_words(vr + b * 32 * P, vw);
+#pragma unroll
+      for (int t = 0; t < P; ++t) acc = C::mac(acc, run_at<Val>(vw, t), xs, (int)cw[t]);
+    }
+    k = nb * P;  // the stride-32 tail runs in the loops below
+  } else if constexpr (P > 0) {
     const int nb = steps / P, k0 = nb * P;
     int tc[TL];
     Val tv[TL];
@@ -400,8 +469,10 @@ bool launch_mixed(const SlicedMatrix& m, const SlicedMixed& mx, const void* xs, 
     set_error("sliced: too many tasks for one launch");
     return false;
   }
-  // Lane runs (FP32 form): 4 steps, 16 bytes of values.
-  constexpr int R = std::is_same<typename C::Val, float>::value ? 4 : 0;
+  // Lane runs: 16 bytes of values (FP32 form 4 steps, BF16 form 8 steps).
+  constexpr int R = std::is_same<typename C::Val, float>::value            ? 4
+                    : std::is_same<typename C::Val, unsigned short>::value ? 8
+                                                                            : 0;
   if (m.lane_run != 0 && m.lane_run != R) {
     set_error("sliced: lane runs do not match the precision form");
     return false;

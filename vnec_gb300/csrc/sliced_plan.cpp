@@ -365,16 +365,17 @@ std::unique_ptr<Plan> upload(std::unique_ptr<SlicedPlan> p, SlicedHost* h, int v
     vals = conv.data();
   }
   const size_t eb = evb * hv.vpe;
-  // FP32 form: lane runs of 4 steps (16 bytes of values).  By default where
-  // most entries sit in 16-bit-delta tasks (local columns, stream-bound: the
-  // 256^3 stencil runs 11% faster); gather-bound layouts keep stride 32.
+  // FP32 / BF16 forms: lane runs of 16 bytes of values (4 / 8 steps).  By
+  // default where most entries sit in 16-bit-delta tasks (local columns,
+  // stream-bound: the 256^3 stencil runs 11% / 7% faster); gather-bound
+  // layouts keep stride 32.
   std::vector<int32_t> col_runs;
   std::vector<uint16_t> col16_runs;
   const int32_t* cols = hv.col;
   const uint16_t* col16 = hv.col16;
   int run = 0;
   const int lv = opts ? opts->lane_vectors : 0;
-  if (prec == kPrecFP32 && hv.vpe == 1 && lv >= 0) {
+  if ((prec == kPrecFP32 || prec == kPrecBF16) && hv.vpe == 1 && lv >= 0) {
     int64_t delta_entries = 0;
     bool aligned = true;
     for (int64_t t = 0; t < hv.num_tasks; ++t) {
@@ -383,11 +384,14 @@ std::unique_ptr<Plan> upload(std::unique_ptr<SlicedPlan> p, SlicedHost* h, int v
       if (k.meta & kSlicedDelta) delta_entries += (int64_t)k.steps * 32;
       if (k.base % 32 != 0) aligned = false;  // vector loads need bases aligned to 32 entries
     }
-    if (aligned && (lv > 0 || 2 * delta_entries >= hv.entries)) run = 4;
+    if (aligned && (lv > 0 || 2 * delta_entries >= hv.entries)) run = prec == kPrecFP32 ? 4 : 8;
   }
   if (run) {
     const size_t ne = (size_t)(hv.entries + pad);
-    to_lane_runs(hv, run, reinterpret_cast<float*>(conv.data()));
+    if (prec == kPrecFP32)
+      to_lane_runs(hv, run, reinterpret_cast<float*>(conv.data()));
+    else
+      to_lane_runs(hv, run, reinterpret_cast<uint16_t*>(conv.data()));
     col_runs.assign(hv.col, hv.col + ne);
     to_lane_runs(hv, run, col_runs.data());
     cols = col_runs.data();
