@@ -482,6 +482,41 @@ def test_sliced_lane_vectors(built, kw, prec):
         check_f64(ys[1], m, xv, tol=PREC_TOL[prec])
 
 
+@pytest.mark.parametrize("fp64", [True, False], ids=["fp64", "fp32"])
+def test_sliced_long_rows_chunked(built, fp64):
+    """Rows longer than the grouping limit run as chunks whose sums the fix-up
+    launch adds in chunk order: repeated calls, host calls split into
+    row-window parts and the fused y := a A x + b z + c epilogue all give the
+    oracle's answer and the same bits call after call."""
+    import torch
+
+    from vnec_gb300 import api
+    from vnec_gb300 import generators as G
+
+    dt = np.float64 if fp64 else np.float32
+    m = G.lognormal(60000, sigma=2.2, cap=20000, seed=21)
+    xv = G.vector(m.n_cols, seed=22).astype(dt)
+    for kw in (dict(long_row_len=32), dict(long_row_len=256, window_rows=4096), dict(long_row_len=1024)):
+        p = api.Plan(m, dtype=dt, kernel=api.KERNEL_S, **kw)
+        y0 = p.mxv_host(xv)
+        (check_f64 if fp64 else check_f32)(y0, m, xv)
+        for _ in range(3):
+            assert p.mxv_host(xv).tobytes() == y0.tobytes()
+        x = torch.from_numpy(xv).cuda()
+        y = torch.empty(m.n_rows, dtype=x.dtype, device="cuda")
+        for _ in range(3):
+            p.mxv_device(x.data_ptr(), y.data_ptr())
+            torch.cuda.synchronize()
+            assert y.cpu().numpy().tobytes() == y0.tobytes()
+        z = torch.from_numpy(G.vector(m.n_rows, seed=23).astype(dt)).cuda()
+        p.mxv_axpby(x.data_ptr(), y.data_ptr(), 2.0, -0.5, z.data_ptr(), 0.25)
+        torch.cuda.synchronize()
+        want = 2.0 * y0.astype(np.float64) - 0.5 * z.cpu().numpy().astype(np.float64) + 0.25
+        tol = 1e-12 if fp64 else 1e-5
+        np.testing.assert_allclose(y.cpu().numpy(), want, rtol=tol, atol=tol)
+        p.free()
+
+
 def test_sliced_full_size_rmat_scale24(built):
     from vnec_gb300 import api
     from vnec_gb300 import generators as G
