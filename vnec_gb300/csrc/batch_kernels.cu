@@ -33,6 +33,7 @@
 
 #include "batch.h"
 #include "common.h"
+#include "df32.cuh"
 
 namespace vnec {
 namespace {
@@ -129,16 +130,11 @@ struct CodecDF32 {
   }
   __device__ static A zero() { return A{0.f, 0.f}; }
   __device__ static void mac(A& a, V v, X x) {
-    const float p = __fmul_rn(v.x, x.x);
-    const float e = fmaf(v.x, x.x, -p);
-    const float q = fmaf(v.x, x.y, fmaf(v.y, x.x, e));
-    const float t = __fadd_rn(a.s, p);
-    const float bb = __fsub_rn(t, a.s);
-    const float r = __fadd_rn(__fsub_rn(a.s, __fsub_rn(t, bb)), __fsub_rn(p, bb));
-    a.s = t;
-    a.c = __fadd_rn(a.c, __fadd_rn(r, q));
+    const DF r = df_mac(DF{a.s, a.c}, v.x, v.y, x.x, x.y);
+    a.s = r.s;
+    a.c = r.c;
   }
-  __device__ static double out(const A& a) { return static_cast<double>(a.s) + static_cast<double>(a.c); }
+  __device__ static double out(const A& a) { return df_to_f64(DF{a.s, a.c}); }
 };
 
 // FP64 from split values and FP64 X: the guard path of DF32 plans.

@@ -39,6 +39,7 @@
 #include <cstdint>
 
 #include "common.h"
+#include "df32.cuh"
 #include "ptx.cuh"
 
 namespace vnec {
@@ -46,39 +47,11 @@ namespace {
 
 constexpr unsigned kFull = 0xffffffffu;
 
-struct DF {
-  float s, c;  // value = s + c, |c| <= ulp(s) after renormalisation
-};
-
 __device__ __forceinline__ DF df_add(DF a, DF b) {
   float t = __fadd_rn(a.s, b.s);
   float bb = __fsub_rn(t, a.s);
   float r = __fadd_rn(__fsub_rn(a.s, __fsub_rn(t, bb)), __fsub_rn(b.s, bb));
   return DF{t, __fadd_rn(__fadd_rn(a.c, b.c), r)};
-}
-
-// Truncation split of a double into hi + lo floats (integer operations only).
-// Returns false when v is outside the supported range (nonzero |v| must lie in
-// [2^-40, 2^41) and be finite).
-__device__ __forceinline__ bool split_f64(double v, float& hi, float& lo) {
-  const unsigned long long b = static_cast<unsigned long long>(__double_as_longlong(v));
-  const unsigned sign = static_cast<unsigned>(b >> 63) << 31;
-  const int e = static_cast<int>((b >> 52) & 0x7ff);
-  const unsigned long long m = b & 0xFFFFFFFFFFFFFull;
-  if (e == 0 && m == 0) {
-    hi = 0.0f;
-    lo = 0.0f;
-    return true;
-  }
-  const int E = e - 1023;
-  const bool ok = (E >= -40) && (E <= 40);
-  hi = __uint_as_float(sign | (static_cast<unsigned>(E + 127) << 23) | static_cast<unsigned>(m >> 29));
-  const unsigned rem = static_cast<unsigned>(m & 0x1FFFFFFFull);
-  const int msb = 31 - __clz(rem | 1u);  // 0..28 (rem==0 handled below)
-  const unsigned mant = msb > 23 ? (rem >> (msb - 23)) : (rem << (23 - msb));
-  const int ex = E - 52 + msb + 127;
-  lo = rem ? __uint_as_float(sign | (static_cast<unsigned>(ex) << 23) | (mant & 0x7FFFFFu)) : 0.0f;
-  return ok;
 }
 
 struct ModeF64 {
@@ -97,19 +70,13 @@ struct ModeDF32 {
   __device__ static Acc zero() { return DF{0.0f, 0.0f}; }
   __device__ static Acc mac(Acc acc, double a, double x, bool& bad) {
     float ah, al, xh, xl;
-    bool ok = split_f64(a, ah, al);
-    ok &= split_f64(x, xh, xl);
+    bool ok = df_split(a, ah, al);
+    ok &= df_split(x, xh, xl);
     bad |= !ok;
-    const float p = __fmul_rn(ah, xh);
-    const float e = fmaf(ah, xh, -p);                 // exact: ah*xh = p + e
-    const float q = fmaf(ah, xl, fmaf(al, xh, e));    // low-order part of the product
-    const float t = __fadd_rn(acc.s, p);              // TwoSum(acc.s, p)
-    const float bb = __fsub_rn(t, acc.s);
-    const float r = __fadd_rn(__fsub_rn(acc.s, __fsub_rn(t, bb)), __fsub_rn(p, bb));
-    return DF{t, __fadd_rn(acc.c, __fadd_rn(r, q))};
+    return df_mac(acc, ah, al, xh, xl);
   }
   __device__ static Acc add(Acc a, Acc b) { return df_add(a, b); }
-  __device__ static double to_f64(Acc a) { return static_cast<double>(a.s) + static_cast<double>(a.c); }
+  __device__ static double to_f64(Acc a) { return df_to_f64(a); }
   __device__ static Acc shfl_up(Acc v, int d) {
     return DF{__shfl_up_sync(kFull, v.s, d), __shfl_up_sync(kFull, v.c, d)};
   }

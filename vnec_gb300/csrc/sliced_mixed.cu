@@ -27,6 +27,7 @@
 #include <type_traits>
 
 #include "common.h"
+#include "df32.cuh"
 #include "sliced.h"
 #include "vnec_gb300.h"
 
@@ -76,29 +77,6 @@ __device__ __forceinline__ float f64_to_f32_rne(double v) {
   return __uint_as_float(sign | bits);
 }
 
-// Truncation split of a double into hi + lo floats; false when a nonzero v
-// lies outside [2^-40, 2^41) (both halves and their products must stay
-// normal FP32 numbers).
-__device__ __forceinline__ bool split_df(double v, float& hi, float& lo) {
-  const unsigned long long b = static_cast<unsigned long long>(__double_as_longlong(v));
-  const unsigned sign = static_cast<unsigned>(b >> 63) << 31;
-  const int e = static_cast<int>((b >> 52) & 0x7ff);
-  const unsigned long long m = b & 0xFFFFFFFFFFFFFull;
-  if (e == 0 && m == 0) {
-    hi = 0.0f;
-    lo = 0.0f;
-    return true;
-  }
-  const int E = e - 1023;
-  const bool ok = (E >= -40) && (E <= 40);
-  hi = __uint_as_float(sign | (static_cast<unsigned>(E + 127) << 23) | static_cast<unsigned>(m >> 29));
-  const unsigned rem = static_cast<unsigned>(m & 0x1FFFFFFFull);
-  const int msb = 31 - __clz(rem | 1u);
-  const unsigned mant = msb > 23 ? (rem >> (msb - 23)) : (rem << (23 - msb));
-  lo = rem ? __uint_as_float(sign | (static_cast<unsigned>(E - 52 + msb + 127) << 23) | (mant & 0x7FFFFFu)) : 0.0f;
-  return ok;
-}
-
 }  // namespace
 
 // Outside the anonymous namespace: also launched by SpB_VNEC_f64_to_f32_ext.
@@ -128,15 +106,11 @@ __global__ void x_split_kernel(const double* __restrict__ x, float2* __restrict_
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n + nh;
        i += (long long)gridDim.x * blockDim.x) {
     float h, l;
-    bad |= !split_df(x_ext(x, n, hot, i), h, l);
+    bad |= !df_split(x_ext(x, n, hot, i), h, l);
     xs[i] = make_float2(h, l);
   }
   if (__syncthreads_or(bad) && threadIdx.x == 0) atomicExch(flag, 1);
 }
-
-struct DF {
-  float s, c;
-};
 
 struct CodecF32 {
   using Val = float;
@@ -163,17 +137,10 @@ struct CodecDF32 {
   using Acc = DF;
   __device__ static Acc zero() { return DF{0.0f, 0.0f}; }
   __device__ static Acc mac(Acc acc, Val v, const void* xs, int c) {
-    const float ah = v.x, al = v.y;
     const float2 x = __ldg(static_cast<const float2*>(xs) + c);
-    const float p = __fmul_rn(ah, x.x);
-    const float e = fmaf(ah, x.x, -p);              // ah*xh = p + e exactly
-    const float q = fmaf(ah, x.y, fmaf(al, x.x, e));
-    const float t = __fadd_rn(acc.s, p);            // TwoSum(acc.s, p)
-    const float bb = __fsub_rn(t, acc.s);
-    const float r = __fadd_rn(__fsub_rn(acc.s, __fsub_rn(t, bb)), __fsub_rn(p, bb));
-    return DF{t, __fadd_rn(acc.c, __fadd_rn(r, q))};
+    return df_mac(acc, v.x, v.y, x.x, x.y);
   }
-  __device__ static double to_f64(Acc a) { return static_cast<double>(a.s) + static_cast<double>(a.c); }
+  __device__ static double to_f64(Acc a) { return df_to_f64(a); }
 };
 
 template <typename T> __device__ __forceinline__ T ld_stream(const T* p) { return __ldcs(p); }
