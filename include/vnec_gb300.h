@@ -220,7 +220,10 @@ SpB_Info SpB_mxv_host_ext(void *plan, const void *h_x, void *h_y);
  * previous call's SpMV and its y copy the next call's, so a sequence of
  * calls runs at the rate of its slowest stage.  h_x must not change and h_y
  * must not be read until SpB_VNEC_host_wait_ext returns; page-locked host
- * buffers are needed for the copies to overlap.  Works with every plan kind. */
+ * buffers are needed for the copies to overlap.  Works with every plan kind.
+ * A synchronous host call on the plan (SpB_mxv_host_ext, SpB_mxv) first waits
+ * for the pipelined SpMVs in flight; device-pointer calls on the plan go after
+ * SpB_VNEC_host_wait_ext. */
 SpB_Info SpB_mxv_host_async_ext(void *plan, const void *h_x, void *h_y);
 /* Waits for every enqueued pipelined call of the plan and reports device-side
  * errors (as SpB_VNEC_device_status_ext). */

@@ -45,11 +45,15 @@ def test_async_host_calls_match_sync(built, kind, pinned):
         p.host_wait()
         for i in range(n):
             assert hy[i].tobytes() == want[i].tobytes(), (rep, i)
-    # a synchronous call between pipelined ones
-    p.mxv_host_async(hx[0], hy[0])
+    # a synchronous call while pipelined ones are in flight (it waits for
+    # their SpMVs: they share the plan's scratch)
+    for i in range(2, n):
+        hy[i].fill(np.nan)
+        p.mxv_host_async(hx[i], hy[i])
     assert p.mxv_host(xs[1]).tobytes() == want[1].tobytes()
     p.host_wait()
-    assert hy[0].tobytes() == want[0].tobytes()
+    for i in range(2, n):
+        assert hy[i].tobytes() == want[i].tobytes(), i
     p.free()
 
 
@@ -72,15 +76,27 @@ def test_async_host_calls_batch_plan(built):
         bp.free()
 
 
-def test_async_rejects_wrong_dtype(built):
+def test_host_calls_reject_bad_arrays(built):
+    """Wrong dtype, wrong size or read-only y is refused before anything is
+    enqueued (a short host buffer would be overrun by the copies)."""
     from vnec_gb300 import api
     from vnec_gb300 import generators as G
 
     m = G.uniform_k(1000, 5, seed=1)
     p = api.Plan(m, kernel=api.KERNEL_S)
+    x, y = np.zeros(m.n_cols), np.zeros(m.n_rows)
+    ro = np.zeros(m.n_rows)
+    ro.flags.writeable = False
+    bad = [(np.zeros(m.n_cols, dtype=np.float32), y), (x[:-1], y), (x, y[:-1]), (x, ro)]
+    for bx, by in bad:
+        with pytest.raises(ValueError):
+            p.mxv_host_async(bx, by)
     with pytest.raises(ValueError):
-        p.mxv_host_async(np.zeros(m.n_cols, dtype=np.float32), np.zeros(m.n_rows))
+        p.mxv_host(x[:-1])
+    with pytest.raises(ValueError):
+        p.mxv_host(x, y[:-1])
     p.host_wait()  # nothing enqueued
+    assert p.mxv_host(x, y) is y
     p.free()
 
 

@@ -410,25 +410,45 @@ class Plan:
         _check(lib().SpB_mxv_axpby_ext(self.h, d_x, d_y, alpha, beta, d_z or None, gamma, stream or None)
                == SpB_SUCCESS, "SpB_mxv_axpby_ext")
 
+    def _host_sizes(self) -> tuple[int, int]:
+        """Values of x and of y one host-vector call copies (n_cols and n_rows
+        times the right-hand sides)."""
+        inf = self.info()
+        r = max(int(inf.rhs), 1)
+        return inf.n_cols * r, inf.n_rows * r
+
+    def _check_y(self, y: np.ndarray, ny: int) -> None:
+        if y.dtype != self.dtype or not y.flags.c_contiguous or not y.flags.writeable or y.size != ny:
+            raise ValueError(f"y must be a writeable contiguous array of {ny} values of the plan's value type")
+
     def mxv_host(self, x: np.ndarray, y: np.ndarray | None = None) -> np.ndarray:
-        inf_rows = self.info().n_rows
+        nx, ny = self._host_sizes()
         x = np.ascontiguousarray(x, dtype=self.dtype)
+        if x.size != nx:
+            raise ValueError(f"x must hold {nx} values")
         if y is None:
-            y = np.empty(inf_rows, dtype=self.dtype)
+            y = np.empty(ny, dtype=self.dtype)
+        self._check_y(y, ny)
         _check(lib().SpB_mxv_host_ext(self.h, x.ctypes.data, y.ctypes.data) == SpB_SUCCESS, "SpB_mxv_host_ext")
         return y
 
     def mxv_host_async(self, x: np.ndarray, y: np.ndarray) -> None:
         """Enqueues y := A x on the pipelined host path (SpB_mxv_host_async_ext);
-        x and y must be contiguous arrays of the plan's type that stay alive and
-        untouched until host_wait() returns."""
-        if x.dtype != self.dtype or y.dtype != self.dtype or not (x.flags.c_contiguous and y.flags.c_contiguous):
-            raise ValueError("x and y must be contiguous arrays of the plan's value type")
+        x and y are contiguous arrays of the plan's type, left untouched until
+        host_wait() returns (the plan holds references to them until then)."""
+        nx, ny = self._host_sizes()
+        if x.dtype != self.dtype or not x.flags.c_contiguous or x.size != nx:
+            raise ValueError(f"x must be a contiguous array of {nx} values of the plan's value type")
+        self._check_y(y, ny)
         _check(lib().SpB_mxv_host_async_ext(self.h, x.ctypes.data, y.ctypes.data) == SpB_SUCCESS,
                "SpB_mxv_host_async_ext")
+        self.__dict__.setdefault("_in_flight", []).append((x, y))
 
     def host_wait(self) -> None:
-        _check(lib().SpB_VNEC_host_wait_ext(self.h) == SpB_SUCCESS, "SpB_VNEC_host_wait_ext")
+        try:
+            _check(lib().SpB_VNEC_host_wait_ext(self.h) == SpB_SUCCESS, "SpB_VNEC_host_wait_ext")
+        finally:
+            self.__dict__.pop("_in_flight", None)
 
     def spmspv_host(self, idx: np.ndarray, val: np.ndarray, y: np.ndarray | None = None) -> np.ndarray:
         """y = A x for sparse x (push plans): idx int32 positions, val values."""
@@ -458,8 +478,9 @@ class Plan:
 
     def free(self) -> None:
         if self.h:
-            lib().SpB_VNEC_plan_free_ext(self.h)
+            lib().SpB_VNEC_plan_free_ext(self.h)  # waits for pipelined calls in flight
             self.h = None
+        self.__dict__.pop("_in_flight", None)
 
     def __del__(self):  # pragma: no cover
         try:
@@ -525,6 +546,7 @@ class BatchPlan(Plan):
             raise ValueError("x must hold n_cols * k values")
         if y is None:
             y = np.empty((inf.n_rows, self.k), dtype=np.float64)
+        self._check_y(y, inf.n_rows * self.k)
         _check(lib().SpB_mxv_host_ext(self.h, x.ctypes.data, y.ctypes.data) == SpB_SUCCESS, "SpB_mxv_host_ext")
         return y
 

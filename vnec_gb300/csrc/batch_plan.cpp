@@ -396,6 +396,7 @@ struct BatchPlan final : Plan {
   bool run_host(const void* h_x, void* h_y) override {
     if (parts.size() < 2 || profiling) return Plan::run_host(h_x, h_y);
     std::lock_guard<std::mutex> g(host_mu);
+    if (!drain_pipe()) return false;
     const size_t row_bytes = sizeof(double) * (size_t)rhs;
     if (!own_stream && !VNEC_CUDA(cudaStreamCreateWithFlags(&own_stream, cudaStreamNonBlocking))) return false;
     if (!in_stream && !VNEC_CUDA(cudaStreamCreateWithFlags(&in_stream, cudaStreamNonBlocking))) return false;

@@ -251,6 +251,7 @@ bool Plan::run_epilogue(const void* d_x, void* d_y, const SlicedEpilogue& e, cud
 
 bool Plan::run_host(const void* h_x, void* h_y) {
   std::lock_guard<std::mutex> g(host_mu);
+  if (!drain_pipe()) return false;
   const size_t vb = type == SpB_FP64 ? 8 : 4;
   if (!own_stream && !VNEC_CUDA(cudaStreamCreateWithFlags(&own_stream, cudaStreamNonBlocking))) return false;
   const size_t nx = (size_t)n_cols * rhs, ny = (size_t)n_rows * rhs;

@@ -100,6 +100,9 @@ struct Plan {
   // call i's SpMV.  host_wait() waits for every enqueued call.
   bool run_host_async(const void* h_x, void* h_y);
   bool host_wait();
+  // Waits for the SpMVs of pipelined calls still in flight (they share the
+  // plan's scratch with a synchronous host call); caller holds host_mu.
+  bool drain_pipe() { return !pipe || VNEC_CUDA(cudaStreamSynchronize(pipe->comp)); }
   // The SpMV of one pipelined call (slot 0 or 1); default run().
   virtual bool run_slot(int slot, const void* d_x, void* d_y, cudaStream_t s) {
     (void)slot;

@@ -96,6 +96,7 @@ bool push_run_sparse_host(Plan* p, long long nx, const int32_t* idx, const void*
   }
   auto* q = static_cast<PushPlan*>(p);
   std::lock_guard<std::mutex> g(q->host_mu);
+  if (!q->drain_pipe()) return false;
   const size_t vb = q->type == SpB_FP64 ? 8 : 4;
   if (!q->own_stream && !VNEC_CUDA(cudaStreamCreateWithFlags(&q->own_stream, cudaStreamNonBlocking))) return false;
   if (q->sx_idx.bytes < sizeof(int32_t) * (size_t)std::max<long long>(nx, 1)) {

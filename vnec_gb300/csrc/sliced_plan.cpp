@@ -95,6 +95,7 @@ struct SlicedPlan final : Plan {
   bool run_host(const void* h_x, void* h_y) override {
     if (mx.precision != kPrecFP64 || m.vpe != 1 || parts.size() < 2 || profiling) return Plan::run_host(h_x, h_y);
     std::lock_guard<std::mutex> g(host_mu);
+    if (!drain_pipe()) return false;
     const size_t vb = type == SpB_FP64 ? 8 : 4;
     if (!own_stream && !VNEC_CUDA(cudaStreamCreateWithFlags(&own_stream, cudaStreamNonBlocking))) return false;
     if (!copy_stream && !VNEC_CUDA(cudaStreamCreateWithFlags(&copy_stream, cudaStreamNonBlocking))) return false;
