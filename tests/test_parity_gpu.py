@@ -96,6 +96,41 @@ def test_spb_mxv_auto_plan_and_cache(built):
     api.lib().SpB_VNEC_forget_ext(A.handle)
 
 
+def test_spb_mxv_concurrent_first_calls(built):
+    """First SpB_mxv calls on one matrix from several host threads at once:
+    each builds a plan, one is kept in the cache (the others are dropped, none
+    that a caller is running), and every thread gets the same y."""
+    import threading
+
+    from vnec_gb300 import api
+    from vnec_gb300 import generators as G
+
+    m = G.lognormal(40000, seed=5)
+    xv = G.vector(m.n_cols, seed=6)
+    A = api.Matrix.from_csr(m)
+    x = api.Vector(xv)
+    ys = [api.Vector(n=m.n_rows) for _ in range(4)]
+    errors = []
+
+    def worker(t):
+        try:
+            for _ in range(3):
+                api.SpB_mxv(ys[t], A, x)
+        except Exception as e:  # noqa: BLE001 - reported below
+            errors.append(repr(e))
+
+    threads = [threading.Thread(target=worker, args=(t,)) for t in range(len(ys))]
+    for th in threads:
+        th.start()
+    for th in threads:
+        th.join()
+    assert not errors, errors
+    check_f64(ys[0].values, m, xv)
+    for y in ys[1:]:
+        assert y.values.tobytes() == ys[0].values.tobytes()
+    api.lib().SpB_VNEC_forget_ext(A.handle)
+
+
 UNPIPELINED = [(128, 4), (128, 7), (128, 10), (256, 4), (256, 7), (256, 10)]
 PIPELINED = [(256, 7, 2), (256, 7, 3), (256, 12, 2), (128, 12, 3), (512, 5, 2)]
 

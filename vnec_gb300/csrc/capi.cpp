@@ -197,10 +197,18 @@ Plan* plan_for_mxv(const SpB_Matrix A, void* handle) {
   if (!view_from_matrix(A, &v)) return nullptr;
   std::unique_ptr<Plan> p = build_from_view(v, nullptr);
   if (!p) return nullptr;
-  Plan* raw = p.get();
+  std::unique_ptr<Plan> stale;  // freed after the lock is released
   std::lock_guard<std::mutex> g(g_cache_mu);
-  auto_cache()[A] = std::make_pair(k, std::move(p));
-  return raw;
+  auto& slot = auto_cache()[A];
+  // A concurrent first call on the same matrix may have cached its plan
+  // meanwhile: keep that one (its caller may be running it) and drop ours.
+  if (slot.second && same_key(slot.first, k)) {
+    stale = std::move(p);
+    return slot.second.get();
+  }
+  stale = std::move(slot.second);
+  slot = std::make_pair(k, std::move(p));
+  return slot.second.get();
 }
 
 SpB_Info run_mxv(SpB_Vector y, const SpB_Matrix A, const SpB_Vector x, Plan* p) {
@@ -486,8 +494,12 @@ void SpB_VNEC_plan_free_ext(void* plan) {
 }
 
 void SpB_VNEC_forget_ext(const SpB_Matrix A) {
+  std::unique_ptr<Plan> stale;  // freed after the lock is released
   std::lock_guard<std::mutex> g(g_cache_mu);
-  auto_cache().erase(A);
+  auto it = auto_cache().find(A);
+  if (it == auto_cache().end()) return;
+  stale = std::move(it->second.second);
+  auto_cache().erase(it);
 }
 
 SpB_Info SpB_mxv_device_ext(void* plan, const void* d_x, void* d_y, void* stream) {
