@@ -854,3 +854,9 @@ def test_f64_to_f32_rounding_matches_hardware(built):
     nan = np.isnan(ref)
     assert np.array_equal(np.isnan(got), nan)
     assert np.array_equal(got[~nan].view(np.uint32), ref[~nan].view(np.uint32))
+    # x 8 bytes past a 16-byte boundary (one value per step instead of four)
+    out1 = torch.empty(allv.size - 1, dtype=torch.float32, device="cuda")
+    assert api.lib().SpB_VNEC_f64_to_f32_ext(d.data_ptr() + 8, out1.data_ptr(), allv.size - 1, None) == api.SpB_SUCCESS
+    got1 = out1.cpu().numpy()
+    assert np.array_equal(np.isnan(got1), nan[1:])
+    assert np.array_equal(got1[~nan[1:]].view(np.uint32), ref[1:][~nan[1:]].view(np.uint32))

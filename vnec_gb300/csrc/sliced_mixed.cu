@@ -79,11 +79,6 @@ __device__ __forceinline__ float f64_to_f32_rne(double v) {
 
 }  // namespace
 
-// Outside the anonymous namespace: also launched by SpB_VNEC_f64_to_f32_ext.
-__global__ void x_to_f32_kernel(const double* __restrict__ x, float* __restrict__ x32, long long n) {
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
-    x32[i] = f64_to_f32_rne(x[i]);
-}
 namespace {
 
 // x (n values) followed by the values of the `nh` hot columns (a plan with a
@@ -93,18 +88,53 @@ __device__ __forceinline__ double x_ext(const double* __restrict__ x, long long 
   return x[i < n ? i : __ldg(hot + (i - n))];
 }
 
-__global__ void x_to_f32_ext_kernel(const double* __restrict__ x, float* __restrict__ x32, long long n,
-                                    const int32_t* __restrict__ hot, int nh) {
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n + nh;
-       i += (long long)gridDim.x * blockDim.x)
-    x32[i] = f64_to_f32_rne(x_ext(x, n, hot, i));
+__device__ __forceinline__ bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15) == 0; }
+
+// x rounded to FP32, then the hot columns' values.  Each thread rounds four
+// consecutive values per step (two 16-byte loads, one 16-byte store) when x is
+// 16-byte aligned, so enough bytes are in flight to run at HBM rate; the
+// remainder and the hot tail take one value per step.
+__device__ __forceinline__ void round_x(const double* __restrict__ x, float* __restrict__ x32, long long n,
+                                        const int32_t* __restrict__ hot, int nh) {
+  const long long t0 = blockIdx.x * (long long)blockDim.x + threadIdx.x, nt = (long long)gridDim.x * blockDim.x;
+  const long long n4 = aligned16(x) && aligned16(x32) ? n / 4 : 0;
+  for (long long q = t0; q < n4; q += nt) {
+    const double2 a = __ldcs(reinterpret_cast<const double2*>(x) + 2 * q);
+    const double2 b = __ldcs(reinterpret_cast<const double2*>(x) + 2 * q + 1);
+    reinterpret_cast<float4*>(x32)[q] =
+        make_float4(f64_to_f32_rne(a.x), f64_to_f32_rne(a.y), f64_to_f32_rne(b.x), f64_to_f32_rne(b.y));
+  }
+  for (long long i = 4 * n4 + t0; i < n + nh; i += nt) x32[i] = f64_to_f32_rne(x_ext(x, n, hot, i));
 }
 
+}  // namespace
+
+// Outside the anonymous namespace: also launched by SpB_VNEC_f64_to_f32_ext.
+__global__ void x_to_f32_kernel(const double* __restrict__ x, float* __restrict__ x32, long long n) {
+  round_x(x, x32, n, nullptr, 0);
+}
+namespace {
+
+__global__ void x_to_f32_ext_kernel(const double* __restrict__ x, float* __restrict__ x32, long long n,
+                                    const int32_t* __restrict__ hot, int nh) {
+  round_x(x, x32, n, hot, nh);
+}
+
+// x split into (hi, lo) pairs, then the hot columns' pairs: two values per
+// step (one 16-byte load, one 16-byte store) when x is 16-byte aligned.
 __global__ void x_split_kernel(const double* __restrict__ x, float2* __restrict__ xs, long long n, int* flag,
                                const int32_t* __restrict__ hot, int nh) {
+  const long long t0 = blockIdx.x * (long long)blockDim.x + threadIdx.x, nt = (long long)gridDim.x * blockDim.x;
+  const long long n2 = aligned16(x) && aligned16(xs) ? n / 2 : 0;
   bool bad = false;
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n + nh;
-       i += (long long)gridDim.x * blockDim.x) {
+  for (long long q = t0; q < n2; q += nt) {
+    const double2 a = __ldcs(reinterpret_cast<const double2*>(x) + q);
+    float h0, l0, h1, l1;
+    bad |= !df_split(a.x, h0, l0);
+    bad |= !df_split(a.y, h1, l1);
+    reinterpret_cast<float4*>(xs)[q] = make_float4(h0, l0, h1, l1);
+  }
+  for (long long i = 2 * n2 + t0; i < n + nh; i += nt) {
     float h, l;
     bad |= !df_split(x_ext(x, n, hot, i), h, l);
     xs[i] = make_float2(h, l);
