@@ -363,7 +363,8 @@ def run_ours(args) -> None:
     prec = PRECISIONS[args.precision]
     if prec != api.PREC_FP64 and args.kernel != "S":
         raise SystemExit("--precision applies to the sliced kernel (--kernel S)")
-    plan = api.Plan(m, kernel=kernel, items_per_thread=-1 if args.kernel == "S" else 0, precision=prec)
+    plan = api.Plan(m, kernel=kernel, items_per_thread=-1 if args.kernel == "S" else 0, precision=prec,
+                    shared_patterns=0 if args.shared_patterns == "on" else -1)
     t_plan = time.time() - t_plan
     info = plan.info()
     stream = torch.cuda.Stream(device=dev)
@@ -448,7 +449,8 @@ def run_ours(args) -> None:
     # columns (plus a first column per row) where 16-bit deltas are used.
     B_form = info.algorithmic_bytes if args.kernel in ("S", "D") else B
     achieved = B_form / (np.mean(main_ms) / 1e3) / 1e9
-    traffic = profiled_traffic(kname, args.workload + ("" if prec == api.PREC_FP64 else "_" + args.precision))
+    traffic = profiled_traffic(kname, args.workload + ("" if prec == api.PREC_FP64 else "_" + args.precision) +
+                               ("_noshared" if prec != api.PREC_FP64 and args.shared_patterns == "off" else ""))
     line = {
         "metric": METRIC, "value": round(value, 3), "unit": "GB/s", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(total_ms / args.steps, 5), "higher_is_better": True,
@@ -457,6 +459,7 @@ def run_ours(args) -> None:
         "config": {"workload": desc + ("" if prec == api.PREC_FP64 else f"_{args.precision}_form"),
                    "n_rows": m.n_rows, "n_cols": m.n_cols, "nnz": m.nnz,
                    "algorithmic_bytes": B, "form_bytes": B_form,
+                   "shared_patterns": args.shared_patterns if prec != api.PREC_FP64 else "n/a",
                    "value_bytes": "plain FP64 bytes (value and e2e are time ratios across forms)",
                    "kernel": {"L": "merge-path CSR (VNEC-L counterpart)",
                               "S": "sliced row groups (VNEC-S counterpart)",
@@ -741,6 +744,8 @@ def main() -> None:
                     help="flush L2 before each timed step (default) or keep it warm (small workloads' warm figure)")
     ap.add_argument("--precision", default="fp64", choices=list(PRECISIONS),
                     help="sliced-kernel form of the main plan (the headline is fp64)")
+    ap.add_argument("--shared-patterns", default="on", choices=["on", "off"],
+                    help="precision forms: one copy of the column gaps for row groups that share them (default on)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-legs", action="store_true", help="skip the precision-form / tuner / batch legs")
     ap.add_argument("--no-batch-leg", action="store_true", help="skip the batched-form legs of the default run")

@@ -170,7 +170,10 @@ typedef struct {
                             (bit-identical to the plan without a window) */
   int offsets64;         /* merge-path plans: 1 stores row ends and merge coordinates as 64-bit
                             integers (always done from 2^31 - 1 rows + nonzeros on) */
-  int reserved[6];
+  int shared_patterns;   /* sliced precision forms: groups of rows with equal length and the
+                            same column gaps (stencils, banded rows) read one copy of the gaps
+                            per group (0: on, -1: off; the sums are the same either way) */
+  int reserved[5];
 } SpB_VNEC_options_ext;
 
 /* Precision forms of the sliced kernel for an FP64 matrix (x and y stay

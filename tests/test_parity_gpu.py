@@ -517,6 +517,45 @@ def test_sliced_lane_vectors(built, kw, prec):
         check_f64(ys[1], m, xv, tol=PREC_TOL[prec])
 
 
+@pytest.mark.parametrize("kw", [dict(), dict(lane_vectors=-1), dict(lane_vectors=1), dict(max_steps=7),
+                                dict(unroll=4), dict(unroll=8), dict(unroll=16)],
+                         ids=["default", "stride32", "runs", "steps7", "u4", "u8", "u16"])
+@pytest.mark.parametrize("prec", [1, 2, 3], ids=["fp32", "bf16_rowscale", "df32"])
+def test_sliced_shared_patterns(built, kw, prec):
+    """Tasks whose rows share one column pattern (stencil interiors, equal
+    rows of a constant band) read the pattern once per task and form each
+    step's column as the row's first column plus a warp-shuffled offset: y is
+    bit-identical to the per-lane deltas, and the stencil's algorithmic bytes
+    drop by the per-lane delta stream."""
+    from vnec_gb300 import api
+    from vnec_gb300 import generators as G
+
+    kw = dict(kw)
+    u = kw.pop("unroll", 12)
+    kw.setdefault("max_steps", 32)
+    band = _custom(5000, 5000, [9] * 5000)  # random columns: nothing shared
+    n = 6000  # constant offsets, clipped at the edges: interior rows share one pattern
+    rows = [np.unique(np.clip(r + np.array([-40, -3, -1, 0, 2, 7, 300]), 0, n - 1)) for r in range(n)]
+    ptr = np.zeros(n + 1, dtype=np.int64)
+    ptr[1:] = np.cumsum([len(c) for c in rows])
+    const = G.from_arrays(n, n, ptr, np.concatenate(rows).astype(np.int32),
+                          np.random.default_rng(4).uniform(-1, 1, int(ptr[-1])))
+    for m in (G.stencil27(20, seed=3), G.stencil27(3, seed=1), const, band,
+              G.lognormal(20000, sigma=1.3, cap=900, seed=5)):
+        xv = G.vector(m.n_cols, seed=8)
+        ys, nbytes = [], []
+        for sp in (-1, 0):
+            p = api.Plan(m, kernel=api.KERNEL_S, precision=prec, shared_patterns=sp, items_per_thread=u, **kw)
+            ys.append(p.mxv_host(xv))
+            nbytes.append(p.info().algorithmic_bytes)
+            p.free()
+        assert ys[0].tobytes() == ys[1].tobytes()
+        check_f64(ys[1], m, xv, tol=PREC_TOL[prec])
+        assert nbytes[1] <= nbytes[0]
+        if m.n_rows == 8000 and kw["max_steps"] == 32:  # 20^3 stencil, one row per lane: 5,832 interior rows
+            assert nbytes[1] < nbytes[0] - m.nnz
+
+
 @pytest.mark.parametrize("fp64", [True, False], ids=["fp64", "fp32"])
 def test_sliced_long_rows_chunked(built, fp64):
     """Rows longer than the grouping limit run as chunks whose sums the fix-up

@@ -67,7 +67,7 @@ class Options(C.Structure):
                 ("precision", C.c_int), ("hot_columns", C.c_int), ("dense_fill_permille", C.c_int),
                 ("transpose", C.c_int), ("host_parts", C.c_int), ("column_deltas", C.c_int),
                 ("lane_vectors", C.c_int), ("hot_order", C.c_int), ("offsets64", C.c_int),
-                ("reserved", C.c_int * 6)]
+                ("shared_patterns", C.c_int), ("reserved", C.c_int * 5)]
 
 
 class Info(C.Structure):
@@ -358,7 +358,8 @@ def options(kernel: int = KERNEL_AUTO, threads_per_block: int = 0, items_per_thr
             pipeline_stages: int = 0, arithmetic: int = ARITH_AUTO, window_rows: int = 0, long_row_len: int = 0,
             max_steps: int = 0, cache_hints: int = 0, precision: int = PREC_FP64, hot_columns: int = 0,
             dense_fill_permille: int = 0, transpose: bool = False, host_parts: int = 0,
-            column_deltas: int = 0, lane_vectors: int = 0, hot_order: int = 0, offsets64: int = 0) -> Options:
+            column_deltas: int = 0, lane_vectors: int = 0, hot_order: int = 0, offsets64: int = 0,
+            shared_patterns: int = 0) -> Options:
     o = Options()
     o.kernel, o.threads_per_block, o.items_per_thread = kernel, threads_per_block, items_per_thread
     o.pipeline_stages, o.arithmetic = pipeline_stages, arithmetic
@@ -371,6 +372,7 @@ def options(kernel: int = KERNEL_AUTO, threads_per_block: int = 0, items_per_thr
     o.lane_vectors = lane_vectors
     o.hot_order = hot_order
     o.offsets64 = offsets64
+    o.shared_patterns = shared_patterns
     return o
 
 

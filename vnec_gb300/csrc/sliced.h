@@ -20,6 +20,11 @@ enum SlicedKind : int { kSlicedRows = 0, kSlicedChunk = 1, kSlicedZero = 2 };
 // deltas: lane g starts at first[row_base + g] and adds col16[entry] at each
 // step (0 on padding), so the column stream costs 2 bytes per entry instead of 4.
 constexpr int kSlicedDelta = 1 << 16;
+// meta flag of a delta task whose rows all have `steps` entries with the same
+// deltas (stencils, banded rows): the deltas are also stored once for the task,
+// step k at pat16[base / 32 + k] (step 0: 0), for kernels that read the task's
+// columns as first[row_base + g] plus a per-step offset shared by all lanes.
+constexpr int kSlicedShared = 1 << 17;
 
 struct SlicedTask {
   int32_t base;      // first entry (element index into vals / cols)
@@ -51,6 +56,7 @@ struct SlicedMatrix {
   bool hot_ready = false;             // xhot already gathered for this call (later parts of a split call)
   const uint16_t* col16 = nullptr;    // delta tasks (kSlicedDelta): 16-bit column deltas
   const int32_t* first = nullptr;     // delta tasks: first column of each row slot
+  const uint16_t* pat16 = nullptr;    // shared-pattern tasks (kSlicedShared): one delta per step
   // FP32 / BF16 forms: 0, or P when val / col / col16 hold each lane's entries
   // in runs of P consecutive steps.  Steps [P*b, P*b + P) of a task's lane l
   // sit at base + b*32*P + l*P + (step - P*b), so a lane reads a run with one
@@ -66,6 +72,7 @@ struct SlicedParams {
   int max_steps = 32;         // target load steps per lane for grouped rows
   int hot = 0;                // hot-column window size (0: none)
   bool delta16 = false;       // 16-bit column deltas for VW = 1 groups whose rows allow it
+  bool shared = false;        // delta16 layouts: also mark shared-pattern tasks (kSlicedShared)
   // Optional secondary key of the row sort (rows of equal length in a window
   // are grouped in ascending key order), n_rows values, or null.
   const int32_t* row_key = nullptr;
@@ -102,6 +109,8 @@ struct SlicedHostView {
   const int64_t* win_long;
   const int64_t* win_entry;
   int64_t delta_nnz, delta_rows;  // nonzeros and rows stored with 16-bit column deltas
+  const uint16_t* pat16;          // shared-pattern deltas (entries / 32 + 64), or null
+  int64_t shared_nnz, shared_steps;  // nonzeros and steps of shared-pattern tasks
 };
 SlicedHostView sliced_view(const SlicedHost* h);
 

@@ -34,6 +34,8 @@ struct SlicedHost {
   std::vector<int32_t> rowid, long_row, long_first;
   std::unique_ptr<uint16_t[]> col16;  // delta16 layouts only
   std::vector<int32_t> first;
+  std::unique_ptr<uint16_t[]> pat16;  // shared-pattern deltas (delta16 + shared layouts)
+  int64_t shared_nnz = 0, shared_steps = 0;
 };
 
 namespace {
@@ -169,10 +171,16 @@ SlicedHost* sliced_build(int64_t n_rows, int64_t /*n_cols*/, const int64_t* rp, 
     h->col16.reset(new uint16_t[(size_t)(h->entries + pad)]);
     std::memset(h->col16.get(), 0, sizeof(uint16_t) * (size_t)(h->entries + pad));
     h->first.assign((size_t)std::max<int64_t>(h->n_rowid, 1), 0);
+    if (prm.shared) {
+      const size_t np = (size_t)(h->entries / 32 + pad);
+      h->pat16.reset(new uint16_t[np]);
+      std::memset(h->pat16.get(), 0, sizeof(uint16_t) * np);
+    }
   }
 
   // Pass 2: global task list and the interleaved entries.
   std::vector<int64_t> win_dnnz((size_t)nwin, 0), win_drows((size_t)nwin, 0);
+  std::vector<int64_t> win_snnz((size_t)nwin, 0), win_ssteps((size_t)nwin, 0);
 #pragma omp parallel for schedule(dynamic, 1)
   for (int64_t w = 0; w < nwin; ++w) {
     Window& wd = win[(size_t)w];
@@ -235,7 +243,31 @@ SlicedHost* sliced_build(int64_t n_rows, int64_t /*n_cols*/, const int64_t* rp, 
             win_dnnz[(size_t)w] += len;
           }
           win_drows[(size_t)w] += nrows;
-          h->tasks[(size_t)(off_t[w] + (int64_t)ti)].meta |= kSlicedDelta;
+          int meta = kSlicedDelta;
+          // Shared pattern: every row has `steps` entries and the first row's
+          // deltas (at most 32 steps: one lane per step holds the pattern).
+          bool shared = h->pat16 && nrows > 0 && t.steps <= 32 && t.base % 32 == 0;
+          const int64_t b0 = shared ? begin(h->rowid[(size_t)t.row_base]) : 0;
+          for (int g = 0; g < nrows && shared; ++g) {
+            const int64_t b = begin(h->rowid[(size_t)(t.row_base + g)]);
+            if (begin(h->rowid[(size_t)(t.row_base + g)] + 1) - b != t.steps) {
+              shared = false;
+              break;
+            }
+            for (int64_t j = 1; j < t.steps; ++j)
+              if (colat(b + j) - colat(b + j - 1) != colat(b0 + j) - colat(b0 + j - 1)) {
+                shared = false;
+                break;
+              }
+          }
+          if (shared) {
+            uint16_t* pd = h->pat16.get() + t.base / 32;
+            for (int64_t j = 1; j < t.steps; ++j) pd[j] = (uint16_t)(colat(b0 + j) - colat(b0 + j - 1));
+            win_snnz[(size_t)w] += (int64_t)nrows * t.steps;
+            win_ssteps[(size_t)w] += t.steps;
+            meta |= kSlicedShared;
+          }
+          h->tasks[(size_t)(off_t[w] + (int64_t)ti)].meta |= meta;
         }
       } else {  // chunk of a long row
         const int32_t r = wd.long_row[li];
@@ -257,6 +289,8 @@ SlicedHost* sliced_build(int64_t n_rows, int64_t /*n_cols*/, const int64_t* rp, 
   for (int64_t w = 0; w < nwin; ++w) {
     h->delta_nnz += win_dnnz[(size_t)w];
     h->delta_rows += win_drows[(size_t)w];
+    h->shared_nnz += win_snnz[(size_t)w];
+    h->shared_steps += win_ssteps[(size_t)w];
   }
   return h;
 }
@@ -285,6 +319,9 @@ SlicedHostView sliced_view(const SlicedHost* h) {
   v.win_entry = h->win_entry.data();
   v.delta_nnz = h->delta_nnz;
   v.delta_rows = h->delta_rows;
+  v.pat16 = h->pat16.get();
+  v.shared_nnz = h->shared_nnz;
+  v.shared_steps = h->shared_steps;
   return v;
 }
 

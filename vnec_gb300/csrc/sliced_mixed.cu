@@ -218,13 +218,16 @@ __device__ __forceinline__ double pow2(int e) {
 // P > 0: the arrays hold lane runs of P steps (SlicedMatrix::lane_run);
 // 2U / P runs are in flight per lane.  The per-lane sums take the same steps
 // in the same order as the stride-32 layout (P = 0), so both give the same y.
-template <class C, int U, int P>
+// SH: the plan has shared-pattern tasks (kSlicedShared); plans without them
+// run the SH = false build, whose registers the shared path does not raise.
+template <class C, int U, int P, bool SH>
 __global__ void __launch_bounds__(kWarps * 32)
 sliced_mixed_kernel(const SlicedTask* __restrict__ tasks, long long num_tasks, const typename C::Val* __restrict__ val,
                     const int32_t* __restrict__ col, const int32_t* __restrict__ rowid, const void* __restrict__ xs,
                     double* __restrict__ y, double* __restrict__ chunk_sum, const signed char* __restrict__ row_scale,
                     const signed char* __restrict__ chunk_scale, const int* __restrict__ flag,
-                    const uint16_t* __restrict__ col16, const int32_t* __restrict__ first) {
+                    const uint16_t* __restrict__ col16, const int32_t* __restrict__ first,
+                    const uint16_t* __restrict__ pat16) {
   if (flag && *reinterpret_cast<const volatile int*>(flag)) return;  // DF32: x out of range, guard launch computes
   const long long w = ((long long)blockIdx.x * kWarps) + (threadIdx.x >> 5);
   const int lane = threadIdx.x & 31;
@@ -246,6 +249,88 @@ sliced_mixed_kernel(const SlicedTask* __restrict__ tasks, long long num_tasks, c
   // and sum the ragged tail in a final loop: fewer registers, more warps.
   constexpr bool kSerialTail = sizeof(Val) == 2;
   constexpr int UBS = U / 4 > 0 ? U / 4 : 1;
+  if (SH && (meta & kSlicedShared)) {
+    // Every row of the task has `steps` entries with the same column gaps:
+    // lane k loads gap k of the shared pattern, a warp prefix sum turns the
+    // gaps into offsets from the first column, and step k's column is the
+    // row's first column plus offset k (a shuffle; no load on the x path).
+    int off = lane < steps ? __ldg(pat16 + (base >> 5) + lane) : 0;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int t = __shfl_up_sync(0xffffffffu, off, o);
+      if (lane >= o) off += t;
+    }
+    const int c0 = lane < nrows ? __ldg(first + row_base + lane) : 0;
+    typename C::Acc acc = C::zero();
+    const Val* vp = val + base + lane;
+    if constexpr (P > 0 && kSerialTail) {
+      // BF16 runs: UBS runs at a time, then single runs, then the tail one
+      // step at a time (fewer registers than a preloaded 7-step tail).
+      const int nb = steps / P;
+      const Val* vr = val + base + lane * P;
+      int b = 0;
+      for (; b + UBS <= nb; b += UBS) {
+        uint32_t vw[UBS][VW];
+#pragma unroll
+        for (int u = 0; u < UBS; ++u) ld_words(vr + (b + u) * 32 * P, vw[u]);
+#pragma unroll
+        for (int u = 0; u < UBS; ++u)
+#pragma unroll
+          for (int t = 0; t < P; ++t)
+            acc = C::mac(acc, run_at<Val>(vw[u], t), xs, c0 + __shfl_sync(0xffffffffu, off, (b + u) * P + t));
+      }
+      for (; b < nb; ++b) {
+        uint32_t vw[VW];
+        ld_words(vr + b * 32 * P, vw);
+#pragma unroll
+        for (int t = 0; t < P; ++t)
+          acc = C::mac(acc, run_at<Val>(vw, t), xs, c0 + __shfl_sync(0xffffffffu, off, b * P + t));
+      }
+      for (int k = nb * P; k < steps; ++k)
+        acc = C::mac(acc, ld_stream(vp + k * 32), xs, c0 + __shfl_sync(0xffffffffu, off, k));
+    } else if constexpr (P > 0) {
+      // Lane runs of P steps, UB runs per round (the last round predicated),
+      // then the stride-32 tail, whose values load with the first round.
+      const int nb = steps / P, k0 = nb * P;
+      Val tv[TL];
+#pragma unroll
+      for (int t = 0; t < TL; ++t)
+        if (k0 + t < steps) tv[t] = ld_stream(vp + (k0 + t) * 32);
+      const Val* vr = val + base + lane * P;
+      for (int b = 0; b < nb; b += UB) {
+        uint32_t vw[UB][VW];
+#pragma unroll
+        for (int u = 0; u < UB; ++u)
+          if (b + u < nb) ld_words(vr + (b + u) * 32 * P, vw[u]);
+#pragma unroll
+        for (int u = 0; u < UB; ++u)
+          if (b + u < nb) {
+#pragma unroll
+            for (int t = 0; t < P; ++t)
+              acc = C::mac(acc, run_at<Val>(vw[u], t), xs, c0 + __shfl_sync(0xffffffffu, off, (b + u) * P + t));
+          }
+      }
+#pragma unroll
+      for (int t = 0; t < TL; ++t)
+        if (k0 + t < steps) acc = C::mac(acc, tv[t], xs, c0 + __shfl_sync(0xffffffffu, off, k0 + t));
+    } else {
+      // Chunks of U steps, the last one predicated.
+      for (int k = 0; k < steps; k += U) {
+        Val v[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u)
+          if (k + u < steps) v[u] = ld_stream(vp + (k + u) * 32);
+#pragma unroll
+        for (int u = 0; u < U; ++u)
+          if (k + u < steps) acc = C::mac(acc, v[u], xs, c0 + __shfl_sync(0xffffffffu, off, k + u));
+      }
+    }
+    if (lane < nrows) {
+      const double s = C::to_f64(acc);
+      y[rowid[row_base + lane]] = row_scale ? s * pow2(row_scale[row_base + lane]) : s;
+    }
+    return;
+  }
   if (meta & kSlicedDelta) {
     // One row per lane, columns as 16-bit deltas from the row's first column.
     const Val* vp = val + base + lane;
@@ -474,19 +559,23 @@ bool launch_mixed(const SlicedMatrix& m, const SlicedMixed& mx, const void* xs, 
     set_error("sliced: lane runs do not match the precision form");
     return false;
   }
-  auto pick = [&](auto run) {
+  auto pick_u = [&](auto run, auto sh) {
     constexpr int P = decltype(run)::value;
-    return m.unroll == 4    ? sliced_mixed_kernel<C, 4, P>
-           : m.unroll == 12 ? sliced_mixed_kernel<C, 12, P>
-           : m.unroll == 16 ? sliced_mixed_kernel<C, 16, P>
-                            : sliced_mixed_kernel<C, 8, P>;
+    constexpr bool SH = decltype(sh)::value;
+    return m.unroll == 4    ? sliced_mixed_kernel<C, 4, P, SH>
+           : m.unroll == 12 ? sliced_mixed_kernel<C, 12, P, SH>
+           : m.unroll == 16 ? sliced_mixed_kernel<C, 16, P, SH>
+                            : sliced_mixed_kernel<C, 8, P, SH>;
+  };
+  auto pick = [&](auto run) {
+    return m.pat16 ? pick_u(run, std::true_type{}) : pick_u(run, std::false_type{});
   };
   auto kern = (R > 0 && m.lane_run) ? pick(std::integral_constant<int, R>{}) : pick(std::integral_constant<int, 0>{});
   // DF32 reads the pre-split (hi, lo) pairs; the FP64 values stay for the guard launch.
   const void* vals = std::is_same<typename C::Val, float2>::value ? static_cast<const void*>(mx.val_split) : m.val;
   kern<<<(unsigned)grid, kWarps * 32, 0, s>>>(m.tasks, m.num_tasks, static_cast<const typename C::Val*>(vals), m.col,
                                               m.rowid, xs, y, static_cast<double*>(m.chunk_sum), mx.row_scale,
-                                              mx.chunk_scale, flag, m.col16, m.first);
+                                              mx.chunk_scale, flag, m.col16, m.first, m.pat16);
   return VNEC_CUDA(cudaGetLastError());
 }
 

@@ -17,11 +17,12 @@ struct SlicedPlan final : Plan {
   SlicedMatrix m;
   SlicedMixed mx;  // precision form (FP64 = plain)
   DeviceBuffer tasks, val, col, rowid, long_row, long_first, chunk_sum, xbuf, flag, row_scale, chunk_scale;
-  DeviceBuffer hot_cols, xhot, col16, first, val_split;
+  DeviceBuffer hot_cols, xhot, col16, first, val_split, pat16;
   std::vector<int32_t> hot_host;  // hot-column window: original column of each slot
   SlicedParams prm;
   int64_t blocks = 0;  // dense-block plans: number of blocks of 4
   int64_t delta_nnz = 0, delta_rows = 0;  // stored with 16-bit column deltas (+ a first column per row)
+  int64_t shared_nnz = 0, shared_steps = 0;  // of those, in shared-pattern tasks (one delta per step)
   // Host-vector calls are split into parts (consecutive row windows) so that
   // the copy of one part's y rows to the host overlaps the next part's SpMV.
   struct Part {
@@ -164,7 +165,8 @@ struct SlicedPlan final : Plan {
   int64_t device_bytes() const override {
     return (int64_t)(tasks.bytes + val.bytes + col.bytes + rowid.bytes + long_row.bytes + long_first.bytes +
                      chunk_sum.bytes + xbuf.bytes + flag.bytes + row_scale.bytes + chunk_scale.bytes + dx.bytes +
-                     dy.bytes + hot_cols.bytes + xhot.bytes + col16.bytes + first.bytes + val_split.bytes);
+                     dy.bytes + hot_cols.bytes + xhot.bytes + col16.bytes + first.bytes + val_split.bytes +
+                     pat16.bytes);
   }
   int64_t algorithmic_bytes() const override {
     // Stored value size of the form; x and y stay in the matrix's type.
@@ -174,8 +176,10 @@ struct SlicedPlan final : Plan {
     // Dense-block plans move whole blocks: 4 values and one start column each.
     if (kind == PlanKind::kWindowDense)
       return blocks * (4 * sv + 4) + (n_rows + 1) * 4 + n_cols * io + n_rows * io;
-    // Columns: 4 bytes, or 2 bytes per delta-coded nonzero plus its row's first column.
-    const int64_t cols = 4 * (nnz - delta_nnz) + 2 * delta_nnz + 4 * delta_rows;
+    // Columns: 4 bytes, or 2 bytes per delta-coded nonzero plus its row's first
+    // column; shared-pattern tasks read 2 bytes per step for all their rows.
+    const int64_t cols =
+        4 * (nnz - delta_nnz) + 2 * (delta_nnz - shared_nnz) + 2 * shared_steps + 4 * delta_rows;
     return nnz * sv + cols + (n_rows + 1) * 4 + scale + n_cols * io + n_rows * io;
   }
   void describe(SpB_VNEC_info_ext* info) const override {
@@ -455,6 +459,12 @@ std::unique_ptr<Plan> upload(std::unique_ptr<SlicedPlan> p, SlicedHost* h, int v
     p->m.col16 = p->col16.as<uint16_t>();
     p->m.first = p->first.as<int32_t>();
   }
+  if (hv.col16 && hv.pat16 && hv.shared_steps > 0) {
+    if (!up(p->pat16, hv.pat16, sizeof(uint16_t) * (size_t)(hv.entries / 32 + pad), 0)) return nullptr;
+    p->m.pat16 = p->pat16.as<uint16_t>();
+    p->shared_nnz = hv.shared_nnz;
+    p->shared_steps = hv.shared_steps;
+  }
   SlicedMatrix& m = p->m;
   m.n_rows = p->n_rows;
   m.n_cols = p->n_cols;
@@ -586,6 +596,9 @@ std::unique_ptr<Plan> build_sliced(const CsrView& v, const SpB_VNEC_options_ext*
   // 16-bit column deltas where rows allow them (not with a hot window, whose
   // relabelled columns break the increasing order).
   p->prm.delta16 = p->prm.hot == 0 && !(opts && opts->column_deltas < 0);
+  // Shared-pattern tasks: read by the precision forms' kernel (the FP64
+  // kernel walks the per-lane deltas, which stay stored).
+  p->prm.shared = p->prm.delta16 && prec != kPrecFP64 && !(opts && opts->shared_patterns < 0);
   SlicedHost* h = sliced_build(v.n_rows, v.n_cols, v.ptr, v.ptr64, cols, cols64, src_val, vb, p->prm, 1, keep);
   if (!h) {
     set_error("sliced format: more than 2^31 entries or row slots");
