@@ -155,6 +155,33 @@ def _layout(tmp_path, includes: str, flags: list[str]) -> list[int]:
     return [int(v) for v in subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()]
 
 
+def test_extension_structs_match_c_header(tmp_path):
+    """Every field of the ctypes mirrors of SpB_VNEC_options_ext,
+    SpB_VNEC_info_ext and SpB_VNEC_batch_options_ext sits at the C header's
+    offset, and the sizes agree (new options take reserved slots)."""
+    import subprocess
+
+    from vnec_gb300 import api
+
+    structs = {"SpB_VNEC_options_ext": api.Options, "SpB_VNEC_info_ext": api.Info,
+               "SpB_VNEC_batch_options_ext": api.BatchOptions}
+    lines, want = [], []
+    for cname, py in structs.items():
+        lines.append(f'  printf("%zu\\n", sizeof({cname}));')
+        want.append(C.sizeof(py))
+        for fname, _ in py._fields_:
+            lines.append(f'  printf("%zu\\n", offsetof({cname}, {fname}));')
+            want.append(getattr(py, fname).offset)
+    src = tmp_path / "ext_probe.c"
+    src.write_text('#include <stdio.h>\n#include <stddef.h>\n#include "vnec_gb300.h"\nint main(void) {\n' +
+                   "\n".join(lines) + "\n  return 0;\n}\n")
+    exe = tmp_path / "ext_probe"
+    subprocess.run(["gcc", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True,
+                   capture_output=True)
+    got = [int(v) for v in subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()]
+    assert got == want
+
+
 def test_struct_layout_matches_c_header(tmp_path):
     """The ctypes mirror and include/vnec_spb_types.h lay out identically
     (and, where the reference headers exist, identically to them)."""
