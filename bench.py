@@ -33,8 +33,8 @@ FP32 / DF32, autotuned, 5 graph-replayed steps each).
 `--workload batch512` measures the batched multi-right-hand-side form instead
 (512 uneven matrices, k = 1..32, one graph-replayed persistent launch per step).
 
-Multi-GPU: the path does not partition across GPUs in this build, so N GPUs
-run N independent replicas of the workload (scaling "weak").
+Multi-GPU: one matrix is not partitioned across GPUs, so N GPUs run N
+independent replicas of the workload (scaling "weak").
 
 `--impl reference` times the reference's own CPU algorithm for the path on
 the host cores (the oracle restatement; the reference's AVX-512 build cannot
