@@ -257,6 +257,17 @@ typedef struct {
  * pipeline wait timed out, and clears the status. */
 SpB_Info SpB_VNEC_device_status_ext(void *plan, void *stream);
 
+/* Poll limit of a plan's bounded device waits (no counterpart in the
+ * reference, whose waits are OpenMP barriers).  The pipelined merge-path
+ * kernel polls each pipeline stage's mbarrier at most this many times before
+ * it raises the plan's device error flag, finishes the copies it has in
+ * flight and exits; SpB_VNEC_device_status_ext then reports the timeout.
+ * polls < 0 restores the default (2^24 polls, seconds of wall time); 0 gives
+ * up at the first wait, which is how the timeout path is tested.  Plans
+ * whose kernels never wait accept and ignore it.  Takes effect from the next
+ * call; do not change it while a call of the plan is in flight. */
+SpB_Info SpB_VNEC_wait_polls_ext(void *plan, int64_t polls);
+
 /* Rounds n FP64 values to FP32 (round to nearest even) on `stream`; used for
  * the FP32/BF16 precision forms, exposed for callers keeping x in FP32. */
 SpB_Info SpB_VNEC_f64_to_f32_ext(const double *d_in, float *d_out, int64_t n, void *stream);
@@ -268,18 +279,23 @@ SpB_Info SpB_VNEC_f64_to_f32_ext(const double *d_in, float *d_out, int64_t n, vo
  * latency-critical loops where a cudaMalloc/cudaFree (and the device
  * synchronisation it implies) is not acceptable.  The caller passes the CSR
  * matrix already in device memory — int32 row offsets d_row_ptr[n_rows + 1]
- * with d_row_ptr[n_rows] == nnz, int32 columns < n_cols, FP64 values — and
- * FP64 x and y; the product is enqueued on `stream` (a cudaStream_t, NULL =
- * legacy default stream) with the FP64 merge-path kernel.  Nothing is
- * allocated: the kernel's scratch (tile coordinates and carries) lives in a
- * fixed 5 MiB array that every device holds from library load until process
- * exit.  Limit: n_rows + nnz <= 469,762,048 (262,144 tiles of 1,792 merge
- * items); larger inputs return SpB_FAILURE with a message.  The first call on
- * a device looks up that device's scratch address (cudaGetSymbolAddress), so
- * make a first call on each device before any stream capture.  All calls on a
- * device share the one scratch array: calls that can overlap on the GPU
- * (different streams without ordering) race and must be serialised by the
- * caller. */
+ * with d_row_ptr[0] == 0, non-decreasing, and d_row_ptr[n_rows] == nnz;
+ * int32 columns in [0, n_cols); FP64 values — and FP64 x and y; the product
+ * is enqueued on `stream` (a cudaStream_t, NULL = legacy default stream) with
+ * the FP64 merge-path kernel.  Unlike a plan, this call cannot inspect the
+ * device arrays: offsets that break those rules give wrong y (the kernel's
+ * reads stay inside d_col[0, nnz) and d_val[0, nnz)), and a column outside
+ * [0, n_cols) reads outside x.  Nothing is allocated: the kernel's scratch
+ * (tile coordinates and carries) lives in a fixed 5 MiB array that every
+ * device holds from library load until process exit.  Limit: n_rows, nnz and
+ * n_rows + nnz each <= 469,762,048 (262,144 tiles of 1,792 merge items), and
+ * n_cols <= INT32_MAX; larger inputs return SpB_FAILURE with a message.  The
+ * first call in each CUDA context looks up that context's scratch address
+ * (cudaGetSymbolAddress) and caches it under the context's id, so a device
+ * reset or a caller's own driver context gets its own lookup; make a first
+ * call in each context before any stream capture.  All calls on a device
+ * share the one scratch array: calls that can overlap on the GPU (different
+ * streams without ordering) race and must be serialised by the caller. */
 SpB_Info SpB_mxv_csr_noalloc_ext(int64_t n_rows, int64_t n_cols, int64_t nnz, const int32_t *d_row_ptr,
                                  const int32_t *d_col, const double *d_val, const double *d_x, double *d_y,
                                  void *stream);

@@ -142,6 +142,8 @@ def lib() -> C.CDLL:
     L.SpB_VNEC_kernel_ms_ext.restype = C.c_int
     L.SpB_VNEC_device_status_ext.argtypes = [_vp, _vp]
     L.SpB_VNEC_device_status_ext.restype = C.c_int
+    L.SpB_VNEC_wait_polls_ext.argtypes = [_vp, C.c_int64]
+    L.SpB_VNEC_wait_polls_ext.restype = C.c_int
     L.SpB_VNEC_f64_to_f32_ext.argtypes = [_vp, _vp, C.c_int64, _vp]
     L.SpB_VNEC_f64_to_f32_ext.restype = C.c_int
     L.SpB_VNEC_spmspv_ext.argtypes = [_vp, C.c_int64, _vp, _vp, _vp, _vp]
@@ -469,6 +471,11 @@ class Plan:
     def device_status(self, stream: int = 0) -> None:
         """Raises VnecError if a bounded device wait of this plan timed out."""
         _check(lib().SpB_VNEC_device_status_ext(self.h, stream or None) == SpB_SUCCESS, "device_status")
+
+    def set_wait_polls(self, polls: int = -1) -> None:
+        """Poll limit of the plan's bounded device waits (< 0: default; 0: give
+        up at the first wait)."""
+        _check(lib().SpB_VNEC_wait_polls_ext(self.h, polls) == SpB_SUCCESS, "wait_polls")
 
     def set_profiling(self, on: bool = True) -> None:
         _check(lib().SpB_VNEC_set_profiling_ext(self.h, int(on)) == SpB_SUCCESS, "set_profiling")

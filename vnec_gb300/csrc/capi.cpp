@@ -621,4 +621,15 @@ SpB_Info SpB_VNEC_device_status_ext(void* plan, void* stream) {
   return p->device_status(static_cast<cudaStream_t>(stream)) ? SpB_SUCCESS : SpB_FAILURE;
 }
 
+SpB_Info SpB_VNEC_wait_polls_ext(void* plan, int64_t polls) {
+  clear_error();
+  Plan* p = find_plan(plan);
+  if (!p) {
+    set_error("unknown plan");
+    return SpB_FAILURE;
+  }
+  p->set_wait_polls(polls);
+  return SpB_SUCCESS;
+}
+
 }  // extern "C"

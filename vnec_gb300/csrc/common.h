@@ -142,6 +142,8 @@ size_t mp_smem_bytes(const MpShape& sh, size_t value_bytes);
 constexpr int kMpLaunchesPerCall = 2;
 
 // Pipelined merge-path kernels (mp2_kernels.cu): FP64 values, int32 offsets.
+// Default poll limit of the pipelined kernel's waits (seconds of wall time).
+constexpr int kMp2DefaultWaitPolls = 1 << 24;
 struct Mp2Matrix {
   int64_t n_rows = 0, n_cols = 0, nnz = 0;
   const int* row_end = nullptr;  // padded by >= 4 elements
@@ -156,6 +158,7 @@ struct Mp2Matrix {
   MpShape shape;
   int stages = 2;
   int sms = 0;
+  int wait_polls = kMp2DefaultWaitPolls;  // polls of a pipeline wait before a timeout is reported
 };
 // y = A x.  df32: double-float arithmetic on the FP32 pipe with an F64 guard
 // launch for out-of-range x.  Events as for mp_spmv.

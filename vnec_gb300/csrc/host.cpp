@@ -397,6 +397,9 @@ struct MergePathPlan final : Plan {
     info->pipeline_stages = pipelined ? m2.stages : 0;
     info->arithmetic = type == SpB_FP64 ? (df32 ? SpB_VNEC_ARITH_DF32 : SpB_VNEC_ARITH_FP64) : 0;
   }
+  void set_wait_polls(int64_t polls) override {
+    m2.wait_polls = polls < 0 ? kMp2DefaultWaitPolls : (int)std::min<int64_t>(polls, INT32_MAX);
+  }
   bool device_status(cudaStream_t s) override {
     if (!pipelined) return VNEC_CUDA(cudaStreamSynchronize(s));
     int h[2] = {0, 0};
@@ -517,7 +520,8 @@ std::unique_ptr<Plan> build_merge_path(const CsrView& v, const SpB_VNEC_options_
   if (!VNEC_CUDA(cudaMemset(p->col.as<char>() + 4 * v.nnz, 0, 4 * pad)) ||
       !VNEC_CUDA(cudaMemset(p->val.as<char>() + vb * v.nnz, 0, vb * pad)) ||
       !VNEC_CUDA(cudaMemset(p->row_end.as<char>() + ob * v.n_rows, 0, ob * pad)) ||
-      !VNEC_CUDA(cudaMemset(p->flags.ptr, 0, 64)))
+      !VNEC_CUDA(cudaMemset(p->flags.ptr, 0, 64)) ||
+      !VNEC_CUDA(cudaMemset(p->carry_row.ptr, 0, p->carry_row.bytes)))
     return nullptr;
   m.row_end = p->row_end.ptr;
   m.col = p->col.as<int32_t>();

@@ -91,6 +91,9 @@ struct Plan {
   virtual int kernel_ms(float* ms, int cap) const = 0;
   // Waits for the plan's work on `s` and reports device-side errors.
   virtual bool device_status(cudaStream_t s) { return VNEC_CUDA(cudaStreamSynchronize(s)); }
+  // Poll limit of the plan's bounded device waits (polls < 0: the default);
+  // plans whose kernels never wait ignore it.
+  virtual void set_wait_polls(int64_t polls) { (void)polls; }
   // y := A x with host vectors: copy x in, SpMV, copy y out, synchronise.
   virtual bool run_host(const void* h_x, void* h_y);
   std::mutex host_mu;  // serialises host-vector calls (they share dx, dy and own_stream)

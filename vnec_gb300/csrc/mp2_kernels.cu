@@ -30,8 +30,9 @@
 //           Splitting needs |a|, |x| in [2^-40, 2^41) or zero: the plan checks
 //           A once; a call that meets an x outside that range raises a device
 //           flag and a guard launch recomputes the call in F64 mode.
-// Every mbarrier wait is bounded; on timeout the kernel raises a device error
-// flag, drains its outstanding copies (bounded) and exits.
+// Every mbarrier wait is bounded (Mp2Matrix::wait_polls polls, 2^24 by
+// default); on timeout the kernel raises a device error flag, drains its
+// outstanding copies (bounded by the full limit) and exits.
 
 #include <cuda_runtime.h>
 
@@ -95,6 +96,7 @@ struct Mp2Args {
   int num_tiles;
   int* flags;  // [0]: x outside the DF32 range this call, [1]: pipeline timeout
   int guard;   // 1: this launch only runs when flags[0] is set (F64 recompute)
+  int wait_polls;  // polls of a pipeline wait before it reports a timeout
 };
 
 template <int TPB, int IPT>
@@ -161,7 +163,9 @@ __global__ void __launch_bounds__(TPB) mp2_kernel(const Mp2Args a) {
     cp_async_commit();
   };
 
-  // Drains the copies this CTA still has in flight (bounded) before exiting on an error.
+  // Drains the copies this CTA still has in flight before exiting on an error.
+  // These waits keep the full kSpinLimit whatever a.wait_polls is, so no CTA
+  // leaves while a bulk copy into its shared memory is still running.
   auto drain_and_fail = [&](int k_first_unwaited, int k_end) {
     if (tid == 0) {
       atomicExch(a.flags + 1, 1);
@@ -178,7 +182,7 @@ __global__ void __launch_bounds__(TPB) mp2_kernel(const Mp2Args a) {
   if (tid == 0)
     for (int k = 0; k < S && k < nk; ++k) issue(k);
   {
-    const bool ok = mbar_wait_bounded(&bar[0], 0u, kSpinLimit);
+    const bool ok = mbar_wait_bounded(&bar[0], 0u, a.wait_polls);
     if (__syncthreads_or(!ok)) {
       drain_and_fail(0, nk < S ? nk : S);
       return;
@@ -190,7 +194,7 @@ __global__ void __launch_bounds__(TPB) mp2_kernel(const Mp2Args a) {
   for (int k = 0; k < nk; ++k) {
     const int s = k % S;
     if (k + 1 < nk) {
-      const bool ok = mbar_wait_bounded(&bar[(k + 1) % S], (uint32_t)(((k + 1) / S) & 1), kSpinLimit);
+      const bool ok = mbar_wait_bounded(&bar[(k + 1) % S], (uint32_t)(((k + 1) / S) & 1), a.wait_polls);
       if (__syncthreads_or(!ok)) {
         drain_and_fail(k + 1, (k + S < nk) ? k + S : nk);
         return;
@@ -302,14 +306,17 @@ __global__ void __launch_bounds__(TPB) mp2_kernel(const Mp2Args a) {
 }
 
 // Cross-tile carries (as in mp_kernels.cu), plus reset of the per-call
-// DF32 range flag for the next call.
+// DF32 range flag for the next call.  After a pipeline timeout (flags[1]) the
+// skipped tiles' carry slots hold an earlier call's rows (or the zeros of plan
+// build): the row check keeps every add inside y, whose values the status
+// call then reports as invalid.
 __global__ void mp2_fixup_kernel(const int* __restrict__ carry_row, const double* __restrict__ carry_val,
                                  int num_tiles, int n_rows, double* __restrict__ y, int* flags) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t == 0) flags[0] = 0;
   if (t >= num_tiles) return;
   const int r = carry_row[t];
-  if (r >= n_rows) return;
+  if (r < 0 || r >= n_rows) return;
   if (t > 0 && carry_row[t - 1] == r) return;
   double s = 0.0;
   for (int u = t; u < num_tiles && carry_row[u] == r; ++u) s += carry_val[u];
@@ -339,7 +346,7 @@ template <int TPB, int IPT, int S>
 bool launch_shape(const Mp2Matrix& m, bool df32, const double* x, double* y, cudaStream_t st, cudaEvent_t* ev) {
   Mp2Args args{static_cast<const int*>(m.row_end), m.col, m.val, x, y, static_cast<const int*>(m.tile_row),
                static_cast<const int*>(m.tile_nz), static_cast<int*>(m.carry_row), m.carry_val,
-               (int)m.num_tiles, m.flags, 0};
+               (int)m.num_tiles, m.flags, 0, m.wait_polls};
   if (ev && !VNEC_CUDA(cudaEventRecord(ev[0], st))) return false;
   if (df32) {
     if (!launch_one<ModeDF32, TPB, IPT, S>(args, m.sms, st)) return false;

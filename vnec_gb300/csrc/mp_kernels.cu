@@ -285,6 +285,7 @@ constexpr int kNaTpb = 256, kNaIpt = 7;
 // Scratch capacity: 2^18 tiles of 1,792 merge items, i.e. n_rows + nnz <=
 // 469,762,048; 5,242,888 bytes.
 constexpr long long kNaMaxTiles = 1LL << 18;
+constexpr long long kNaMaxItems = kNaMaxTiles * kNaTpb * kNaIpt;  // 469,762,048
 constexpr size_t kNaTileRowOff = 0;
 constexpr size_t kNaTileNzOff = kNaTileRowOff + 4 * (kNaMaxTiles + 1);
 constexpr size_t kNaCarryRowOff = kNaTileNzOff + 4 * (kNaMaxTiles + 1);
@@ -294,25 +295,71 @@ static_assert(kNaCarryValOff % 8 == 0, "carry values must be 8-byte aligned");
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNaBytes];
 
-// Device address of g_noalloc_scratch for the current device.  In host code
-// the symbol is only a host-side stand-in, so the address is looked up once
-// per device (first call on that device) and cached.
+// Identity of the calling thread's current CUDA context: its driver-assigned
+// id, unique for the life of the process (cuCtxGetId), reached through the
+// runtime's driver entry points so the library needs no link against the
+// driver library.  False when the driver lacks these calls or no context is
+// current yet.
+using CtxGetCurrentFn = int (*)(void**);
+using CtxGetIdFn = int (*)(void*, unsigned long long*);
+bool current_context_id(unsigned long long* id) {
+  static CtxGetCurrentFn get_current = nullptr;
+  static CtxGetIdFn get_id = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_current = reinterpret_cast<CtxGetCurrentFn>(f);
+    f = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_id = reinterpret_cast<CtxGetIdFn>(f);
+  });
+  if (!get_current || !get_id) return false;
+  void* ctx = nullptr;
+  if (get_current(&ctx) != 0 || !ctx) return false;
+  return get_id(ctx, id) == 0;
+}
+
+// Device address of g_noalloc_scratch in the current context.  In host code
+// the symbol is only a host-side stand-in, so the address is looked up with
+// cudaGetSymbolAddress the first time a context calls and cached under that
+// context's id: a device reset or a caller's own driver context gets a new id
+// and therefore its own lookup, never a stale address.  Where the context id
+// cannot be read, the address is looked up on every call.
 bool noalloc_scratch(unsigned char** out) {
+  struct Entry {
+    unsigned long long ctx;
+    unsigned char* addr;
+  };
   static std::mutex mu;
-  static unsigned char* addr[256] = {nullptr};
-  int dev = 0;
-  if (!VNEC_CUDA(cudaGetDevice(&dev))) return false;
-  if (dev < 0 || dev >= 256) {
-    set_error("SpB_mxv_csr_noalloc_ext: device ordinal out of range");
+  static Entry cache[64] = {};
+  static int next = 0;
+  unsigned long long id = 0;
+  bool have_id = current_context_id(&id);
+  if (have_id) {
+    std::lock_guard<std::mutex> g(mu);
+    for (const Entry& e : cache)
+      if (e.addr && e.ctx == id) {
+        *out = e.addr;
+        return true;
+      }
+  }
+  void* p = nullptr;
+  if (!VNEC_CUDA(cudaGetSymbolAddress(&p, g_noalloc_scratch))) return false;
+  if (!p) {
+    set_error("SpB_mxv_csr_noalloc_ext: no device address for the fixed scratch array");
     return false;
   }
-  std::lock_guard<std::mutex> g(mu);
-  if (!addr[dev]) {
-    void* p = nullptr;
-    if (!VNEC_CUDA(cudaGetSymbolAddress(&p, g_noalloc_scratch))) return false;
-    addr[dev] = static_cast<unsigned char*>(p);
+  if (!have_id) have_id = current_context_id(&id);  // the lookup made the primary context current
+  if (have_id) {
+    std::lock_guard<std::mutex> g(mu);
+    cache[next] = Entry{id, static_cast<unsigned char*>(p)};
+    next = (next + 1) % 64;
   }
-  *out = addr[dev];
+  *out = static_cast<unsigned char*>(p);
   return true;
 }
 
@@ -329,12 +376,18 @@ extern "C" SpB_Info SpB_mxv_csr_noalloc_ext(int64_t n_rows, int64_t n_cols, int6
     return SpB_FAILURE;
   }
   const long long ipc = (long long)kNaTpb * kNaIpt;
-  const long long tiles = (n_rows + nnz + ipc - 1) / ipc;
-  if (tiles > kNaMaxTiles) {
+  // Each size is checked on its own before the sum is formed, so huge
+  // arguments cannot overflow it.
+  if (n_rows > kNaMaxItems || nnz > kNaMaxItems || n_rows + nnz > kNaMaxItems) {
     set_error("SpB_mxv_csr_noalloc_ext: n_rows + nnz exceeds the allocation-free limit of 469,762,048 "
               "(its fixed scratch holds 262,144 tiles); use a plan (SpB_VNEC_plan_ext) instead");
     return SpB_FAILURE;
   }
+  if (n_cols > INT32_MAX) {
+    set_error("SpB_mxv_csr_noalloc_ext: n_cols exceeds the int32 column range");
+    return SpB_FAILURE;
+  }
+  const long long tiles = (n_rows + nnz + ipc - 1) / ipc;
   if (n_rows == 0) return SpB_SUCCESS;
   if (!d_row_ptr || !d_y || (nnz > 0 && (!d_col || !d_val || !d_x))) {
     set_error("SpB_mxv_csr_noalloc_ext: NULL device array");
