@@ -196,13 +196,24 @@ def reference_cores_and_parts() -> tuple[int, int, str]:
     return os.cpu_count() or 1, nparts, arch
 
 
-def cpu_time_L(m, x, warm: int, reps: int, budget_s: float) -> tuple[float, int, str]:
-    """Seconds per call of the reference's own dispatch on the host (oracle port):
-    VNEC-L FP64 for n >= 3e6 rows (test_spmv_vnec.cpp:197), else VNEC-S FP64
-    (IRD_VNEC picks S for the sparse configurations timed here)."""
+def cpu_time_L(m, x, warm: int, reps: int, budget_s: float) -> tuple[float, int, str, str]:
+    """Seconds per call of the reference harness's dispatch on the host cores
+    (VNEC-L FP64 for n >= 3e6 rows, else IRD_VNEC's D or S; test_spmv_vnec.cpp:
+    197-256), the timed calls, a description and the kind: "reference" when the
+    reference library built from its own sources for this host is present
+    (oracle/_ref; on the aarch64 GPU host its ARM_NEON build), else "port"
+    (the oracle's restatement with the reference's compile-time constants)."""
     from oracle import oracle as O
 
     cores, nparts, arch = reference_cores_and_parts()
+    if O.ref_available():
+        b = O.ref_build()
+        t1, _ = O.ref_time_f64(m, x, 0, warm, 1)
+        reps = int(max(1, min(reps, budget_s / max(t1, 1e-9))))
+        secs, name = O.ref_time_f64(m, x, 0, 0, reps)
+        flavour = "ARM_NEON" if b is O.ARM else "X86_SIMD (AVX-512)"
+        return secs, reps, (f"{name} FP64 of the reference itself (its {flavour} build, compiled from its own "
+                            f"sources, NUM_THREADS {b['nparts']}) on {cores} {arch} cores"), "reference"
     build = dict(O.ARM if arch in ("aarch64", "arm64") else O.X86, nparts=nparts)
     if m.n_rows >= 3_000_000:
         name = "VNEC-L"
@@ -217,7 +228,8 @@ def cpu_time_L(m, x, warm: int, reps: int, budget_s: float) -> tuple[float, int,
     t1 = run(warm, 1)
     reps = int(max(1, min(reps, budget_s / max(t1, 1e-9))))
     secs = run(0, reps)
-    return secs, reps, f"{name} FP64 restated (oracle port), {nparts} OpenMP partitions/threads on {cores} {arch} cores"
+    return (secs, reps, f"{name} FP64 restated (oracle port), {nparts} OpenMP partitions/threads on {cores} {arch} "
+                        "cores", "port")
 
 
 def time_plan_device(plan, x, y, flush, stream, steps: int, warmup: int) -> list[float]:
@@ -304,6 +316,14 @@ def run_reference(args) -> None:
     ws, rank, _ = dist_env()
     if rank != 0:
         return
+    # Inputs come from the oracle's own build of the seeded generators (same
+    # source, same matrices): this arm maps no library of the product.
+    from oracle import oracle as O
+    from vnec_gb300 import generators as G
+
+    if not os.path.exists(O.GEN_SO):
+        O.build()
+    G.use_library(O.GEN_SO)
     if args.workload == "batch512":
         from vnec_gb300 import generators as G
 
@@ -324,7 +344,8 @@ def run_reference(args) -> None:
     m, x, desc = workload(args.workload)
     B = algorithmic_bytes(m)
     cores, _, _ = reference_cores_and_parts()
-    per_call, reps, how = cpu_time_L(m, x, warm=args.warmup, reps=args.steps, budget_s=max(args.cpu_budget, 60.0))
+    per_call, reps, how, kind = cpu_time_L(m, x, warm=args.warmup, reps=args.steps,
+                                           budget_s=max(args.cpu_budget, 60.0))
     value = B / per_call / 1e9
     sample = (f"full workload, {args.warmup} warm-up + {reps} timed calls of the reference harness's dispatch "
               f"(L for n >= 3e6, else IRD's choice): {how}")
@@ -333,7 +354,7 @@ def run_reference(args) -> None:
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (seeded generator)",
             "config": {"workload": desc, "n_rows": m.n_rows, "nnz": m.nnz, "algorithmic_bytes": B},
-            "cpu_baseline": {"value": round(value, 3), "unit": "GB/s", "cores": cores, "kind": "port",
+            "cpu_baseline": {"value": round(value, 3), "unit": "GB/s", "cores": cores, "kind": kind,
                              "sample": sample},
             "e2e": {"value": round(value, 3), "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -514,9 +535,9 @@ def run_ours(args) -> None:
             for m3 in mats:
                 m3.free()
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
-        secs, reps, sample = cpu_time_L(m, xv, warm=1, reps=40, budget_s=args.cpu_budget)
+        secs, reps, sample, kind = cpu_time_L(m, xv, warm=1, reps=40, budget_s=args.cpu_budget)
         cores, _, _ = reference_cores_and_parts()
-        line["cpu_baseline"] = {"value": round(B / secs / 1e9, 3), "unit": "GB/s", "cores": cores, "kind": "port",
+        line["cpu_baseline"] = {"value": round(B / secs / 1e9, 3), "unit": "GB/s", "cores": cores, "kind": kind,
                                 "sample": f"full workload, 1 warm-up + {reps} calls; {sample}"}
     if rank == 0:
         print(json.dumps(line), flush=True)
@@ -720,18 +741,22 @@ def batch_cpu_baseline(mats, k: int, budget_s: float) -> dict:
     pick = [mats[i] for i in order[::max(1, len(mats) // 32)]]
     t_total, B_total, calls = 0.0, 0, 0
     t_start = time.time()
+    own = O.ref_available()
     for m in pick:
         x = rng.uniform(-1, 1, m.n_cols)
-        t = O.time_L_f64(m, x, nparts, warm=1, reps=3)
+        t = O.ref_time_f64(m, x, 3, warm=1, reps=3)[0] if own else O.time_L_f64(m, x, nparts, warm=1, reps=3)
         t_total += t * k
         B_total += batch_bytes(m.nnz, m.n_rows, m.n_cols, 1, k)
         calls += 4
         if time.time() - t_start > budget_s:
             break
-    return {"value": round(B_total / t_total / 1e9, 3), "unit": "GB/s", "cores": cores, "kind": "port",
-            "sample": f"{len(pick)} of {len(mats)} matrices (evenly spaced in nnz order), SpMV_VNEC_L_FP64 restated "
-                      f"(oracle port) per matrix, 1 warm-up + 3 timed calls, x {k} right-hand sides; "
-                      f"{nparts} OpenMP threads on {cores} {arch} cores"}
+    what = "the reference's own SpMV_VNEC_L_FP64 (its build for this host)" if own else \
+        "SpMV_VNEC_L_FP64 restated (oracle port)"
+    return {"value": round(B_total / t_total / 1e9, 3), "unit": "GB/s", "cores": cores,
+            "kind": "reference" if own else "port",
+            "sample": f"{len(pick)} of {len(mats)} matrices (evenly spaced in nnz order), {what} per matrix, "
+                      f"1 warm-up + 3 timed calls, x {k} right-hand sides; {nparts} OpenMP threads on {cores} "
+                      f"{arch} cores"}
 
 
 def main() -> None:
@@ -763,6 +788,10 @@ def main() -> None:
     args = ap.parse_args()
     if args.warmup < 3:
         raise SystemExit("--warmup must be >= 3")
+    # Thread placement of the reference's own run script (run_vnec.sh:8-9),
+    # for the CPU legs of both arms (set before any OpenMP runtime starts).
+    os.environ.setdefault("OMP_PROC_BIND", "close")
+    os.environ.setdefault("OMP_PLACES", "cores")
     if args.impl == "reference":
         run_reference(args)
     elif args.workload == "batch512":

@@ -7,8 +7,11 @@ baseline; the product library never calls it.
 * ``liboracle.so`` (``vnec_oracle.c``): the C restatement of the reference's
   VNEC path, parameterised by partition count and lane width.
 * ``libvnec_ref.so`` (optional, built from the reference's own sources by
-  ``oracle/Makefile`` target ``ref``, x86 AVX-512 only): used to pin the
-  restatement and to generate the golden fixtures.
+  ``oracle/Makefile`` target ``ref``: the reference's X86_SIMD build on an
+  AVX-512 x86 host, its ARM_NEON build on an aarch64 host): used to pin the
+  restatement, to generate the golden fixtures and, on the aarch64 GPU host,
+  as the timed CPU baseline.  The reference's sources reach a host without
+  the reference checkout as a git-ignored staged archive (``make ref-stage``).
 """
 from __future__ import annotations
 
@@ -21,6 +24,8 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_SO = os.path.join(HERE, "_build", "liboracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libvnec_ref.so")
+REF_TREE = os.path.join(HERE, "_ref", "src-tree")  # the reference's sources unpacked by `make ref`
+GEN_SO = os.path.join(HERE, "_build", "libvnec_gen_oracle.so")
 
 # Compile-time constants of the reference builds (src/operation/include/SpB_mxv.h:17-32).
 X86 = dict(nparts=36, nlanes_f64=8, nlanes_f32=16, thr_f64=0.477, thr_f32=0.437)
@@ -33,10 +38,18 @@ _ref = None
 
 
 def build() -> None:
-    """Builds liboracle.so (and the reference library when its sources exist here)."""
-    subprocess.run(["make", "-s", "-C", HERE], check=True)
-    if os.path.isdir("/root/reference/src/operation/src"):
-        subprocess.run(["make", "-s", "-C", HERE, "ref"], check=True)
+    """Builds liboracle.so, the oracle's copy of the generators and, where the
+    reference's sources are available (checkout or staged archive) and the
+    host has a reference build (AVX-512 x86 or aarch64), the reference library.
+    The reference checkout's location comes from the Makefile (REF, or the
+    VNEC_REFERENCE environment variable)."""
+    subprocess.run(["make", "-s", "-C", HERE, "all", "gen"], check=True)
+    subprocess.run(["make", "-s", "-C", HERE, "ref"], check=True)
+
+
+def reference_tree() -> str | None:
+    """Directory of the reference's sources unpacked by ``make ref``, if any."""
+    return REF_TREE if os.path.isdir(os.path.join(REF_TREE, "src", "core", "src")) else None
 
 
 def lib() -> C.CDLL:
@@ -69,6 +82,11 @@ def ref_available() -> bool:
     return os.path.exists(REF_SO)
 
 
+def ref_build() -> dict:
+    """Constants of the reference build in libvnec_ref.so (X86 or ARM)."""
+    return ARM if ref().ref_num_threads() == ARM["nparts"] else X86
+
+
 def ref() -> C.CDLL:
     global _ref
     if _ref is None:
@@ -80,6 +98,9 @@ def ref() -> C.CDLL:
         R.ref_ird.restype = C.c_int
         R.ref_time_L_f64.argtypes = [_i64, _i64, _i64] + [_vp] * 4 + [C.c_int, C.c_int]
         R.ref_time_L_f64.restype = C.c_double
+        R.ref_time_f64.argtypes = [C.c_int, _i64, _i64, _i64] + [_vp] * 4 + [C.c_int, C.c_int, _vp]
+        R.ref_time_f64.restype = C.c_double
+        R.ref_num_threads.restype = C.c_int
         _ref = R
     return _ref
 
@@ -188,6 +209,18 @@ def ref_spmv(variant: int, m, x, dtype=np.float64) -> tuple[np.ndarray, int, flo
     f = ref().ref_spmv_f64 if dtype == np.float64 else ref().ref_spmv_f32
     used = f(variant, m.n_rows, m.n_cols, m.nnz, _p(rp), _p(ci), _p(v), _p(xx), _p(y), _p(irdv))
     return y, used, float(irdv[0])
+
+
+def ref_time_f64(m, x, variant: int = 0, warm: int = 1, reps: int = 40) -> tuple[float, str]:
+    """Seconds per call of the reference build's own FP64 SpMV (variant 0: the
+    harness's dispatch; 1 D, 2 S, 3 L) and the name of the variant run."""
+    rp, ci = _csr(m)
+    v = np.ascontiguousarray(m.val, dtype=np.float64)
+    xx = np.ascontiguousarray(x, dtype=np.float64)
+    used = np.zeros(1, dtype=np.int32)
+    secs = ref().ref_time_f64(variant, m.n_rows, m.n_cols, m.nnz, _p(rp), _p(ci), _p(v), _p(xx), warm, reps,
+                              _p(used))
+    return float(secs), {1: "VNEC-D", 2: "VNEC-S", 3: "VNEC-L"}.get(int(used[0]), "?")
 
 
 def rowwise_error(y: np.ndarray, y_ref: np.ndarray, cond: np.ndarray) -> np.ndarray:

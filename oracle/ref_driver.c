@@ -217,6 +217,52 @@ int ref_ird(int fp64, int64_t n_rows, int64_t n_cols, int64_t nnz, const int64_t
   return (int)t;
 }
 
+/* Times the reference harness's FP64 path (test_spmv_vnec.cpp:197-256): for
+ * n_rows < 3,000,000 IRD_VNEC picks D or S (variant REF_AUTO; REF_D / REF_S
+ * force one), otherwise VNEC-L; the handle is built once, then `warm` untimed
+ * and `reps` timed back-to-back SpMV calls.  Returns seconds per call;
+ * *used receives the variant run. */
+double ref_time_f64(int variant, int64_t n_rows, int64_t n_cols, int64_t nnz, const int64_t *row_ptr,
+                    const int32_t *col, const double *val, const double *x, int warm, int reps, int *used) {
+  SpB_Matrix G = make_matrix(SpB_FP64, n_rows, n_cols, nnz, row_ptr, col, val);
+  SpB_Vector xv = make_vector(SpB_FP64, n_cols, x);
+  SpB_Vector yv = make_vector(SpB_FP64, n_rows, NULL);
+  if (variant == REF_AUTO) {
+    if (n_rows < 3000000)
+      variant = run_ird(G, SpB_FP64, NULL) == SpB_VNEC_D ? REF_D : REF_S;
+    else
+      variant = REF_L;
+  }
+  if (used) *used = variant;
+  double secs = -1.0;
+  if (variant == REF_D) {
+    VNEC_D_FP64 *h = Build_VNEC_D_FP64(G);
+    for (int i = 0; i < warm; ++i) SpMV_VNEC_D_FP64(yv, G, xv, h);
+    double t0 = omp_get_wtime();
+    for (int i = 0; i < reps; ++i) SpMV_VNEC_D_FP64(yv, G, xv, h);
+    secs = (omp_get_wtime() - t0) / (reps > 0 ? reps : 1);
+    free_d64(h);
+  } else if (variant == REF_S) {
+    VNEC_S_FP64 *h = Build_VNEC_S_FP64(G);
+    for (int i = 0; i < warm; ++i) SpMV_VNEC_S_FP64(yv, G, xv, h);
+    double t0 = omp_get_wtime();
+    for (int i = 0; i < reps; ++i) SpMV_VNEC_S_FP64(yv, G, xv, h);
+    secs = (omp_get_wtime() - t0) / (reps > 0 ? reps : 1);
+    free_s64(h);
+  } else if (variant == REF_L) {
+    VNEC_L *h = Build_VNEC_L(G);
+    for (int i = 0; i < warm; ++i) SpMV_VNEC_L_FP64(yv, G, xv, h);
+    double t0 = omp_get_wtime();
+    for (int i = 0; i < reps; ++i) SpMV_VNEC_L_FP64(yv, G, xv, h);
+    secs = (omp_get_wtime() - t0) / (reps > 0 ? reps : 1);
+    free_l(h);
+  }
+  free_vector(xv);
+  free_vector(yv);
+  free_matrix(G);
+  return secs;
+}
+
 /* Times `reps` back-to-back SpMV_VNEC_L_FP64 calls after one warm-up, as the
  * harness does (test_spmv_vnec.cpp:235-256).  Returns seconds per call. */
 double ref_time_L_f64(int64_t n_rows, int64_t n_cols, int64_t nnz, const int64_t *row_ptr, const int32_t *col,

@@ -174,7 +174,7 @@ def test_batch512_all_forms(built, batch512, k):
         try:
             ro, co = p.offsets()
             X = np.random.default_rng(k).uniform(-1, 1, int(co[-1]) * k)
-            Y = p.mxv_host(X)
+            Y = p.mxv_host(X).reshape(-1)
             for i, (rows, sub) in enumerate(samples):
                 Xi = X[co[i] * k:co[i + 1] * k].reshape(mats[i].n_cols, k)
                 y_ref, cond = O.spmm_neumaier(sub, Xi)

@@ -192,8 +192,10 @@ def test_struct_layout_matches_c_header(tmp_path):
           api._CsrStruct.ptr.offset, api._CsrStruct.nnz.offset, C.sizeof(api._CsrStruct),
           api._DenseStruct.values.offset, mine[7]]
     assert mine == py
-    ref = "/root/reference"
-    if os.path.isdir(os.path.join(ref, "src", "core", "include")):
+    from oracle import oracle as O
+
+    ref = O.reference_tree()
+    if ref:
         theirs = _layout(tmp_path, '#include "SpB_Matrix_CSC_or_CSR.h"\n#include "SpB_Vector_Dense.h"',
                          ["-I", f"{ref}/include", "-I", f"{ref}/src/core/include"])
         assert theirs == mine

@@ -25,3 +25,14 @@ def load(name: str) -> ctypes.CDLL:
         lib = ctypes.CDLL(p)
         _cache[name] = lib
     return lib
+
+
+def load_path(p: str) -> ctypes.CDLL:
+    """Loads a library by file path (cached like `load`)."""
+    lib = _cache.get(p)
+    if lib is None:
+        if not os.path.exists(p):
+            raise LibraryMissing(f"{p} is not built")
+        lib = ctypes.CDLL(p)
+        _cache[p] = lib
+    return lib

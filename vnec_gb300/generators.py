@@ -21,8 +21,22 @@ from . import _loader
 _i64, _i32, _u64, _f64 = C.c_int64, C.c_int32, C.c_uint64, C.c_double
 
 
+_library_path: str | None = None
+
+
+def use_library(path: str) -> None:
+    """Load the generators from another build of ``csrc/generators.cpp`` (the
+    same seeded algorithms, e.g. the oracle's copy, so that a CPU-only run maps
+    no product library).  Must be called before the first generator call."""
+    global _library_path
+    _library_path = path
+
+
 def _lib():
-    lib = _loader.load("vnec_gen")
+    if _library_path is not None:
+        lib = _loader.load_path(_library_path)
+    else:
+        lib = _loader.load("vnec_gen")
     if not getattr(lib, "_vnec_typed", False):
         vp = C.c_void_p
         lib.vnec_gen_uniform_k.argtypes = [_i64, _i64, _i32, _f64, _f64, _u64]
