@@ -4,6 +4,11 @@
   reader accepts (``utilities/reader.hpp:37-150``): 1-based (row, col[, value])
   triples after a size line; ``symmetric`` files are mirrored; ``pattern``
   files get value 1.
+* ``read_mtx_graph`` reads a .mtx file the way the reference's graph reader
+  does before its test harness assigns values (``utilities/reader.hpp:37-163``
+  then ``utilities/builder.hpp:165-185``): the pattern only, 0-based,
+  ``symmetric`` files mirrored, edges sorted, duplicate edges and self-loops
+  removed; values are the harness's (row index).
 * ``read_sg`` / ``write_sg`` follow the serialized CSR the reference's test
   harness loads (``utilities/reader.hpp:189-240``): bool directed, uint64
   num_edges, uint64 num_nodes, uint64 offsets[num_nodes + 1], uint64
@@ -56,6 +61,43 @@ def read_mtx(path: str) -> HostCSR:
         sign = -1.0 if symmetry == "skew-symmetric" else 1.0
         r, c, v = np.concatenate((r, c[off])), np.concatenate((c, r[off])), np.concatenate((v, sign * v[off]))
     return _coo_to_csr(n_rows, n_cols, r, c, v)
+
+
+def read_mtx_graph(path: str, values: np.ndarray | None = None) -> HostCSR:
+    """The graph the reference's Builder makes from a Matrix Market file (the
+    CSR its .mtx -> .sg converter writes): square coordinate matrices only,
+    field pattern / real / double / integer, symmetry general, skew-symmetric
+    (read as general) or symmetric (each entry also read transposed); then
+    sorted, duplicate edges merged into one, self-loops dropped."""
+    with open(path) as f:
+        head = f.readline().split()
+        if len(head) < 5 or head[0] not in ("%%MatrixMarket", "%MatrixMarket"):
+            raise ValueError(f"{path}: .mtx file did not start with %%MatrixMarket or %MatrixMarket")
+        obj, fmt, field, symmetry = head[1], head[2], head[3], head[4]
+        if obj != "matrix" or fmt != "coordinate":
+            raise ValueError(f"{path}: only matrix coordinate format is read")
+        if field not in ("pattern", "real", "double", "integer"):
+            raise ValueError(f"{path}: unsupported field {field!r}")
+        if symmetry not in ("general", "skew-symmetric", "symmetric"):
+            raise ValueError(f"{path}: unsupported symmetry {symmetry!r}")
+        line = f.readline()
+        while line.startswith("%"):
+            line = f.readline()
+        n_rows, n_cols = (int(t) for t in line.split()[:2])
+        if n_rows != n_cols:
+            raise ValueError(f"{path}: matrix must be square")
+        pairs = [tuple(int(t) for t in ln.split()[:2]) for ln in f if ln.strip()]
+    e = np.asarray(pairs, dtype=np.int64).reshape(-1, 2) - 1
+    if symmetry == "symmetric":
+        e = np.concatenate((e, e[:, ::-1]))
+    e = e[e[:, 0] != e[:, 1]]
+    e = np.unique(e, axis=0)  # sorted by (row, column), duplicates merged
+    counts = np.bincount(e[:, 0], minlength=n_rows)
+    row_ptr = np.zeros(n_rows + 1, dtype=np.int64)
+    np.cumsum(counts, out=row_ptr[1:])
+    if values is None:
+        values = np.repeat(np.arange(n_rows, dtype=np.float64), counts)
+    return from_arrays(n_rows, n_cols, row_ptr, e[:, 1], np.asarray(values, dtype=np.float64))
 
 
 def read_sg(path: str, values: np.ndarray | None = None) -> HostCSR:
