@@ -27,9 +27,15 @@ REF_SO = os.path.join(HERE, "_ref", "libvnec_ref.so")
 REF_TREE = os.path.join(HERE, "_ref", "src-tree")  # the reference's sources unpacked by `make ref`
 GEN_SO = os.path.join(HERE, "_build", "libvnec_gen_oracle.so")
 
-# Compile-time constants of the reference builds (src/operation/include/SpB_mxv.h:17-32).
-X86 = dict(nparts=36, nlanes_f64=8, nlanes_f32=16, thr_f64=0.477, thr_f32=0.437)
-ARM = dict(nparts=48, nlanes_f64=2, nlanes_f32=4, thr_f64=0.76, thr_f32=0.543)
+# Compile-time constants of the reference builds (src/operation/include/SpB_mxv.h:17-32),
+# plus how each build's compiler evaluates the multiply-adds (vnec_oracle.c:
+# orc_loop_mode, orc_lane_fused), pinned bit for bit against that build's own
+# outputs: tests/golden/*.npz (X86_SIMD build, x86-64 AVX-512) and
+# tests/golden/arm/*.npz (ARM_NEON build, aarch64 Neoverse V2).
+X86 = dict(nparts=36, nlanes_f64=8, nlanes_f32=16, thr_f64=0.477, thr_f32=0.437,
+           loop_modes=(4, 0, 4, 0, 0, 4, 0, 4, 4, 0), lane_fused=1)
+ARM = dict(nparts=48, nlanes_f64=2, nlanes_f32=4, thr_f64=0.76, thr_f32=0.543,
+           loop_modes=(0, 0, 0, 0, 0, 0, 0, 4, 0, 0), lane_fused=0)
 
 _vp = C.c_void_p
 _i64 = C.c_int64
@@ -105,6 +111,15 @@ def ref() -> C.CDLL:
     return _ref
 
 
+def _use(build: dict) -> None:
+    """Sets the oracle's multiply-add evaluation to that of `build`'s compiler."""
+    L = lib()
+    modes = (C.c_int * len(build["loop_modes"])).in_dll(L, "orc_loop_mode")
+    for i, v in enumerate(build["loop_modes"]):
+        modes[i] = v
+    C.c_int.in_dll(L, "orc_lane_fused").value = build["lane_fused"]
+
+
 def _p(a: np.ndarray) -> int:
     return a.ctypes.data
 
@@ -115,8 +130,9 @@ def _csr(m):
     return rp, ci
 
 
-def spmv_serial(m, x, dtype=np.float64) -> np.ndarray:
+def spmv_serial(m, x, dtype=np.float64, build=X86) -> np.ndarray:
     """SpB_mxv_FP64_serial / _FP32_serial (test_spmv_vnec.hpp:34-79)."""
+    _use(build)
     rp, ci = _csr(m)
     v = np.ascontiguousarray(m.val, dtype=dtype)
     xx = np.ascontiguousarray(x, dtype=dtype)
@@ -152,6 +168,7 @@ def spmm_neumaier(m, X) -> tuple[np.ndarray, np.ndarray]:
 
 def spmv_vnec(variant: str, m, x, dtype=np.float64, build=X86) -> np.ndarray:
     """The restated reference kernels: variant in {'L', 'D', 'S'}."""
+    _use(build)
     rp, ci = _csr(m)
     v = np.ascontiguousarray(m.val, dtype=dtype)
     xx = np.ascontiguousarray(x, dtype=dtype)
@@ -180,8 +197,9 @@ def ird(m, fp64: bool = True, build=X86) -> tuple[int, float]:
     return t, float(out[0])
 
 
-def time_L_f64(m, x, nparts: int, warm: int = 1, reps: int = 40) -> float:
+def time_L_f64(m, x, nparts: int, warm: int = 1, reps: int = 40, build=None) -> float:
     """Seconds per SpMV_VNEC_L_FP64 call of the restatement (OpenMP, nparts threads)."""
+    _use(build or (ARM if nparts == ARM["nparts"] else X86))
     rp, ci = _csr(m)
     v = np.ascontiguousarray(m.val, dtype=np.float64)
     xx = np.ascontiguousarray(x, dtype=np.float64)
@@ -191,6 +209,7 @@ def time_L_f64(m, x, nparts: int, warm: int = 1, reps: int = 40) -> float:
 
 def time_S_f64(m, x, build=ARM, warm: int = 1, reps: int = 40) -> float:
     """Seconds per SpMV_VNEC_S_FP64 call of the restatement (format built once)."""
+    _use(build)
     rp, ci = _csr(m)
     v = np.ascontiguousarray(m.val, dtype=np.float64)
     xx = np.ascontiguousarray(x, dtype=np.float64)

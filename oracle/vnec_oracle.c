@@ -18,10 +18,13 @@
  * use the pairwise tree of the respective intrinsic (restated in
  * reduce_lanes_*).
  *
- * Pinning: tests/test_oracle.py checks the x86 parameterisation bit for bit
- * against outputs of the reference itself (compiled from its own sources by
- * oracle/Makefile into oracle/_ref/, fixtures in tests/golden/).  The ARM
- * parameterisation shares the code but is not pinned against an ARM build.
+ * Pinning: tests/test_oracle.py checks both parameterisations bit for bit
+ * against outputs of the reference itself, compiled from its own sources by
+ * oracle/Makefile into oracle/_ref/: the X86_SIMD build on an AVX-512 x86 host
+ * (fixtures in tests/golden/) and the ARM_NEON build on the aarch64 GPU host
+ * (fixtures in tests/golden/arm/).  The two builds' compilers evaluate the
+ * multiply-adds differently; orc_loop_mode and orc_lane_fused hold each
+ * build's pinned choice (set per call by oracle/oracle.py).
  *
  * Deliberate differences from the reference (none changes arithmetic):
  *   - 64-bit merge coordinates (the reference's `int` coordinates overflow past
@@ -59,6 +62,23 @@ enum {
   LOOP_S_TAIL_F64, LOOP_S_TAIL_F32, LOOP_L_CARRY_F64, LOOP_L_CARRY_F32, LOOP_COUNT
 };
 int orc_loop_mode[LOOP_COUNT] = {4, 0, 4, 0, 0, 4, 0, 4, 4, 0};
+
+/* Lane multiply-accumulate of the D kernels and of the FP32 L kernel's lane
+ * loop.  The x86 build uses _mm512_fmadd_* (fused, 1).  The ARM build uses
+ * vmlaq_f64 / vmlaq_f32 (spmv_vnec_D_for_mxv.c:469, spmv_vnec_L_for_mxv.c:63),
+ * which the ARM build computes as a rounded product followed by a rounded
+ * add (0).  The S kernels use vfmaq / _mm512_fmadd on both builds (fused). */
+int orc_lane_fused = 1;
+static inline double lane_mac_f64(double a, double b, double c) {
+  if (orc_lane_fused) return fma(a, b, c);
+  double p = a * b;
+  return c + p;
+}
+static inline float lane_mac_f32(float a, float b, float c) {
+  if (orc_lane_fused) return fmaf(a, b, c);
+  float p = a * b;
+  return c + p;
+}
 
 static inline double mac_run_f64(int loop, double acc, const double *v, const int32_t *idx, const double *xv, i64 n) {
   int g = orc_loop_mode[loop];
@@ -298,7 +318,7 @@ void orc_spmv_L_f32(int nparts, int nlanes, i64 n_rows, i64 nnz, const i64 *row_
       for (int l = 0; l < nlanes; ++l) lanes[l] = 0.0f;
       i64 loop_end = row_end[cx] - nlanes;
       for (; cy < loop_end; cy += nlanes)
-        for (int l = 0; l < nlanes; ++l) lanes[l] = fmaf(x[col[cy + l]], val[cy + l], lanes[l]);
+        for (int l = 0; l < nlanes; ++l) lanes[l] = lane_mac_f32(x[col[cy + l]], val[cy + l], lanes[l]);
       float rt = reduce_lanes_f32(lanes, nlanes);
       rt = mac_run_f32(LOOP_L_TAIL_F32, rt, val + cy, col + cy, x, row_end[cx] - cy);
       cy = row_end[cx] > cy ? row_end[cx] : cy;
@@ -459,7 +479,7 @@ void orc_spmv_D_f64(int nparts, int nlanes, i64 n_rows, i64 n_cols, i64 nnz, con
         double lanes[16];
         for (int l = 0; l < nlanes; ++l) lanes[l] = 0.0;
         for (i64 b = vrp[i]; b < vrp[i + 1]; ++b)
-          for (int l = 0; l < nlanes; ++l) lanes[l] = fma(va[b * nlanes + l], w[cs[b] + l], lanes[l]);
+          for (int l = 0; l < nlanes; ++l) lanes[l] = lane_mac_f64(va[b * nlanes + l], w[cs[b] + l], lanes[l]);
         y[i] = reduce_lanes_f64(lanes, nlanes);
       }
       double rt = 0.0;
@@ -500,7 +520,7 @@ void orc_spmv_D_f32(int nparts, int nlanes, i64 n_rows, i64 n_cols, i64 nnz, con
         float lanes[32];
         for (int l = 0; l < nlanes; ++l) lanes[l] = 0.0f;
         for (i64 b = vrp[i]; b < vrp[i + 1]; ++b)
-          for (int l = 0; l < nlanes; ++l) lanes[l] = fmaf(va[b * nlanes + l], w[cs[b] + l], lanes[l]);
+          for (int l = 0; l < nlanes; ++l) lanes[l] = lane_mac_f32(va[b * nlanes + l], w[cs[b] + l], lanes[l]);
         y[i] = reduce_lanes_f32(lanes, nlanes);
       }
       float rt = 0.0f;

@@ -7,10 +7,13 @@ at sizes and on machines where the reference itself cannot run.
 """
 from __future__ import annotations
 
+import glob
+import os
+
 import numpy as np
 import pytest
 
-from conftest import golden_cases, golden_csr, golden_manifest, load_golden
+from conftest import GOLDEN, golden_cases, golden_csr, golden_manifest, load_golden
 
 CASES = golden_cases()
 
@@ -49,6 +52,49 @@ def carry_equal(y, y_ref, m, x, nparts: int = 36) -> bool:
         tol = 1e-12 if y.dtype == np.float64 else 1e-5
         return bool(np.all(np.abs(y[racy].astype(np.float64) - y_ref[racy]) <= tol * cond[racy]))
     return True
+
+
+ARM_DIR = os.path.join(GOLDEN, "arm")
+ARM_CASES = sorted(os.path.splitext(os.path.basename(p))[0] for p in glob.glob(os.path.join(ARM_DIR, "*.npz")))
+
+
+def test_arm_manifest_matches_arm_build_constants():
+    """The ARM fixtures come from the reference's ARM_NEON build (NUM_THREADS 48,
+    nLanes 2/4; src/operation/include/SpB_mxv.h:18-24)."""
+    import json
+
+    from oracle import oracle as O
+
+    with open(os.path.join(ARM_DIR, "manifest.json")) as f:
+        rb = json.load(f)["reference_build"]
+    assert (rb["NUM_THREADS"], rb["nLanes_f64"], rb["nLanes_f32"]) == (
+        O.ARM["nparts"], O.ARM["nlanes_f64"], O.ARM["nlanes_f32"])
+    assert set(ARM_CASES) == set(CASES)
+
+
+@pytest.mark.parametrize("case", ARM_CASES)
+@pytest.mark.parametrize("tag,dtype", [("f64", np.float64), ("f32", np.float32)])
+def test_oracle_arm_parameterisation_reproduces_arm_build(built, case, tag, dtype):
+    """The restatement with the ARM build's constants and arithmetic (48
+    partitions, 2/4 lanes, unfused vmlaq lane updates, fused scalar loops)
+    reproduces the reference's ARM_NEON build bit for bit on the golden inputs
+    (rows fed by two or more partitions' carries within 1e-12, as on x86)."""
+    from oracle import oracle as O
+
+    g = load_golden(case)
+    with np.load(os.path.join(ARM_DIR, f"{case}.npz")) as z:
+        a = {k: z[k] for k in z.files}
+    m = golden_csr(g)
+    x = g["x"]
+    nparts = O.ARM["nparts"]
+    assert bits_equal(O.spmv_serial(m, x, dtype=dtype, build=O.ARM), a[f"y_serial_{tag}"])
+    assert carry_equal(O.spmv_vnec("L", m, x, dtype=dtype, build=O.ARM), a[f"y_L_{tag}"], m, x, nparts)
+    if bool(a["vnec_ds_defined"]):
+        assert carry_equal(O.spmv_vnec("D", m, x, dtype=dtype, build=O.ARM), a[f"y_D_{tag}"], m, x, nparts)
+        assert bits_equal(O.spmv_vnec("S", m, x, dtype=dtype, build=O.ARM), a[f"y_S_{tag}"])
+        choice, ratio = O.ird(m, fp64=(tag == "f64"), build=O.ARM)
+        assert abs(ratio - float(a[f"ird_{tag}"])) <= 5.01e-7
+        assert {0: 1, 1: 2}[choice] == int(a[f"auto_variant_{tag}"])
 
 
 def test_manifest_matches_reference_build_constants():
