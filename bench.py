@@ -309,6 +309,28 @@ def form_legs(m, xv, B: int, flush, stream, steps: int, warmup: int) -> dict:
         leg["speedup_vs_fp64"] = round(base / ms, 3)
         legs[name] = leg
         plan.free()
+    # The reference API's own call sequence for matrices of >= 3e6 rows
+    # (test_spmv_vnec.cpp:197,235-256): Build_VNEC_L, then SpMV_VNEC_L_FP64.
+    if m.n_rows >= 3_000_000:
+        t0 = time.time()
+        A = api.Matrix.from_csr(m)
+        h = api.Build_VNEC_L(A)
+        build_s = time.time() - t0
+
+        class _Handle:
+            def mxv_device(self, d_x, d_y, s):
+                api._check(api.lib().SpB_mxv_device_ext(h, d_x, d_y, s or None) == api.SpB_SUCCESS, "mxv")
+
+        try:
+            ms = float(np.median(time_plan_device(_Handle(), x, y, flush, stream, steps, warmup)))
+            rel = O.rowwise_error(y.cpu().numpy(), y_ref, cond)
+            legs["build_vnec_l"] = {"ms": round(ms, 5), "gbs_plain_bytes": round(B / ms / 1e6, 1),
+                                    "max_rel_error": float(rel.max()), "plan_build_s": round(build_s, 2),
+                                    "speedup_vs_fp64": round(base / ms, 3),
+                                    "path": "Build_VNEC_L + SpMV_VNEC_L_FP64 handle (reference API flow)"}
+        finally:
+            api.VNEC_L_free(h)
+            del A
     return legs
 
 

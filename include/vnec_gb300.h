@@ -45,13 +45,27 @@ SpB_Info SpB_mxv(SpB_Vector y, const SpB_Matrix A, const SpB_Vector x, void *VNE
 /* include/OpenSparseBLAS.h:1983 (ird_calc.c:2-122).  Returns SpB_VNEC_D when
  * nnz / (blocks * nLanes) >= threshold, else SpB_VNEC_S, computed exactly as
  * the reference's x86 build does (36 merge-path partitions, nLanes 8/16 and
- * thresholds 0.477/0.437 for FP64/FP32, SpB_mxv.h:25-32).  Does not print. */
+ * thresholds 0.477/0.437 for FP64/FP32, SpB_mxv.h:25-32).  Does not print.
+ * Like the reference (ird_calc.c:103, `int _nnz_ = v_row_ptr[n] * nLanes`),
+ * the denominator blocks x nLanes is a 32-bit int: past 2^31 - 1 (about
+ * 2.7e8 blocks at nLanes 8 — the 27-point stencil on 256^3 has more) it
+ * wraps as the reference's does, so the ratio, and the choice, of such a
+ * matrix is the reference's wrapped one, not a meaningful IRD.  The
+ * reference's harness never asks for it there (it sends every matrix of
+ * 3e6 rows or more to VNEC-L). */
 SpB_VNEC_type IRD_VNEC(const SpB_Matrix A, SpB_Type type);
 
 /* include/OpenSparseBLAS.h:2023 (spmv_vnec_L_for_mxv.c:2-35).  Merge-path plan
- * for A (FP64 or FP32 values).  The public fields num_merge_items and
+ * for A (FP64 or FP32 values) below 2^26 nonzeros; from 2^26 nonzeros on, the
+ * plan of the automatic selection (the one SpB_mxv builds for a NULL handle),
+ * because the reference's harness sends every matrix of 3e6 rows or more to
+ * VNEC-L and the merge-path kernel is the slower plan at those sizes (R-MAT
+ * 2^24: 2.30 vs 0.92 ms).  Either way SpMV_VNEC_L_* computes y := A x within
+ * the same error bound; SpB_VNEC_plan_ext with kernel SpB_VNEC_KERNEL_L gives
+ * a merge-path plan of any size.  The public fields num_merge_items and
  * items_per_thread are filled; the pointer fields are NULL.  Release with
- * VNEC_L_free_ext. */
+ * VNEC_L_free_ext (or the harness's field-by-field free, which leaks the
+ * device plan). */
 struct VNEC_L *Build_VNEC_L(const SpB_Matrix A);
 
 /* include/OpenSparseBLAS.h:2024 and :2073 (spmv_vnec_L_for_mxv.c:36-165). */

@@ -182,3 +182,31 @@ def test_batch512_all_forms(built, batch512, k):
                 _check(Yi, y_ref, cond, TOL[name], f"batch512 k={k} {name} matrix {i}")
         finally:
             p.free()
+
+
+def test_rmat24_reference_flow_through_build_vnec_l(built):
+    """The reference harness's call sequence on the 2^24-row power-law matrix
+    (>= 3e6 rows: Build_VNEC_L + SpMV_VNEC_L_FP64 on host vectors): from 2^26
+    nonzeros on Build_VNEC_L hands back the automatic selection's plan; y must
+    meet 1e-12 row-wise on two calls, and the handle must be released both ways
+    the library allows."""
+    from oracle import oracle as O
+    from vnec_gb300 import api
+    from vnec_gb300 import generators as G
+
+    m = G.rmat(24, 1 << 28, seed=1)
+    xv = G.vector(m.n_cols, seed=1)
+    y_ref, cond = O.spmv_neumaier(m, xv)
+    A = api.Matrix.from_csr(m)
+    x = api.Vector(xv)
+    h = api.Build_VNEC_L(A)
+    try:
+        inf = api.Info()
+        assert api.lib().SpB_VNEC_plan_info_ext(h, api.C.byref(inf)) == api.SpB_SUCCESS
+        assert inf.kernel != api.KERNEL_L  # the selected plan, not the merge path
+        for _ in range(2):
+            y = api.Vector(n=m.n_rows)
+            api.SpMV_VNEC_L_FP64(y, A, x, h)
+            _check(y.values, y_ref, cond, TOL["fp64"], "Build_VNEC_L R-MAT 2^24")
+    finally:
+        api.VNEC_L_free(h)

@@ -623,7 +623,9 @@ float ird_ratio(const CsrView& v, const IrdParams& prm) {
     }
     blocks_total += g;
   }
-  const int denom = (int)(blocks_total * prm.nlanes);
+  // 32-bit, as the reference's `int _nnz_` (ird_calc.c:103): past 2^31 - 1 it
+  // wraps the way the reference's does, so the decision stays the reference's.
+  const int denom = (int)(uint32_t)(blocks_total * prm.nlanes);
   return (float)v.nnz / (float)denom;
 }
 

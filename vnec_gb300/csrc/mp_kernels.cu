@@ -15,16 +15,19 @@
 //      the per-thread loop of the reference's OpenMP threads, at warp lane
 //      granularity;
 //   3. carry: a thread whose segment starts inside a row adds the partial sums
-//      of the preceding threads that stopped in the same row (a walk back over
-//      the shared carry list, one add per carried partial), then writes that
-//      row; the tile's own carry-out (partial of its last row) goes to a
-//      per-tile scratch slot;
+//      of the preceding threads that stopped in the same row, found by a
+//      segmented scan over the threads (warp shuffles plus one scan over the
+//      warp totals, log steps), then writes that row; the tile's own
+//      carry-out (partial of its last row) goes to a per-tile scratch slot;
 //   4. fix-up (second, tiny launch): rows spanning tiles receive the ordered
 //      sum of the carries of the tiles that stopped inside them — the
 //      counterpart of the reference's serial carry loop (:159-164).
-// The FP64 form performs exactly one FP64 FMA per nonzero plus one add per
-// carried partial: on GB300 the FP64 pipe (about 0.6 T FMA/s) is close to the
-// HBM rate for SpMV, so no other FP64 work is done in the loop.
+// The FP64 form performs exactly one FP64 FMA per nonzero plus at most
+// log2(32) + log2(warps) adds per thread for the carries: on GB300 the FP64
+// pipe (about 0.6 T FMA/s) is close to the HBM rate for SpMV, so no other
+// FP64 work is done in the loop.  (A walk back over the preceding threads'
+// partials costs one add per thread a row spans, quadratic in the rows that
+// cover a whole tile: on R-MAT 2^24 it kept the FP64 pipe 70% busy.)
 
 #include <cuda_runtime.h>
 
@@ -73,23 +76,27 @@ __global__ void mp_partition_kernel(const Off* __restrict__ row_end, Off n_rows,
   tile_nz[t] = diag - r;
 }
 
-// One CTA per tile.  Shared memory: s_val[IPC], s_x[IPC] (V), s_carry[TPB] (V),
-// s_end[IPC] (int, row ends relative to the tile's first nonzero), s_emit[TPB].
+// One CTA per tile.  Shared memory: s_val[IPC], s_x[IPC] (V), s_end[IPC]
+// (int, row ends relative to the tile's first nonzero), per-warp carry
+// totals, open flags and carry-ins (TPB / 32 each).
 template <typename V, typename Off, int TPB, int IPT>
 __global__ void __launch_bounds__(TPB)
 mp_spmv_kernel(const Off* __restrict__ row_end, const int32_t* __restrict__ col, const V* __restrict__ val,
                const V* __restrict__ x, V* __restrict__ y, const Off* __restrict__ tile_row,
                const Off* __restrict__ tile_nz, Off* __restrict__ carry_row, V* __restrict__ carry_val) {
   constexpr int IPC = TPB * IPT;
+  constexpr int kW = TPB / 32;
+  constexpr unsigned kFull = 0xffffffffu;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   V* s_val = reinterpret_cast<V*>(smem_raw);
   V* s_x = s_val + IPC;
-  V* s_carry = s_x + IPC;
-  int* s_end = reinterpret_cast<int*>(s_carry + TPB);
-  int* s_emit = s_end + IPC;
+  V* w_run = s_x + IPC;  // [kW] warp totals of the open run
+  V* w_cin = w_run + kW;  // [kW] carry into each warp
+  int* s_end = reinterpret_cast<int*>(w_cin + kW);
+  int* w_open = s_end + IPC;  // [kW]
 
   const int tile = blockIdx.x;
-  const int tid = threadIdx.x;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const Off x0 = tile_row[tile], y0 = tile_nz[tile];
   const Off x1 = tile_row[tile + 1], y1 = tile_nz[tile + 1];
   const int nrows = (int)(x1 - x0);
@@ -137,29 +144,56 @@ mp_spmv_kernel(const Off* __restrict__ row_end, const int32_t* __restrict__ col,
       }
     }
   }
-  s_carry[tid] = acc;
-  s_emit[tid] = first >= 0;
-  __syncthreads();
 
-  // 3. in-tile carries: sum partials of preceding threads that stopped in the
-  // row this thread starts in (they form a run ending at a thread that
-  // emitted a row, or at thread 0).
-  if (first >= 0) {
-    V c = V(0);
-    for (int u = tid - 1; u >= 0; --u) {
-      c += s_carry[u];
-      if (s_emit[u]) break;
+  // 3. in-tile carries.  A thread that emitted a row starts a new run with its
+  // tail partial; a thread that did not is still inside the row of the
+  // threads before it.  A segmented inclusive scan over the threads (warp
+  // shuffles, then one scan over the warp totals) gives every thread the sum
+  // of the open run before it in log steps, however many threads a row spans.
+  V run = acc;
+  int open = first < 0;
+  for (int dist = 1; dist < 32; dist <<= 1) {
+    if (!__ballot_sync(kFull, open && lane >= dist)) break;
+    const V up = __shfl_up_sync(kFull, run, dist);
+    const int up_open = __shfl_up_sync(kFull, open, dist);
+    if (open && lane >= dist) {
+      run += up;
+      open = up_open;
     }
-    y[x0 + first] = first_val + c;
+  }
+  if (lane == 31) {
+    w_run[warp] = run;
+    w_open[warp] = open;
+  }
+  __syncthreads();
+  if (warp == 0) {
+    V cv = lane < kW ? w_run[lane] : V(0);
+    int co = lane < kW ? w_open[lane] : 0;
+    for (int dist = 1; dist < kW; dist <<= 1) {
+      const V up = __shfl_up_sync(kFull, cv, dist);
+      const int up_open = __shfl_up_sync(kFull, co, dist);
+      if (co && lane >= dist) {
+        cv += up;
+        co = up_open;
+      }
+    }
+    const V ex = __shfl_up_sync(kFull, cv, 1);
+    if (lane < kW) w_cin[lane] = lane == 0 ? V(0) : ex;
+  }
+  __syncthreads();
+  const V prev = __shfl_up_sync(kFull, run, 1);
+  const int prev_open = __shfl_up_sync(kFull, open, 1);
+  if (first >= 0) {
+    V cin;
+    if (lane == 0)
+      cin = w_cin[warp];
+    else
+      cin = prev_open ? prev + w_cin[warp] : prev;
+    y[x0 + first] = first_val + cin;
   }
   if (tid == TPB - 1) {
-    V c = V(0);
-    for (int u = TPB - 1; u >= 0; --u) {
-      c += s_carry[u];
-      if (s_emit[u]) break;
-    }
     carry_row[tile] = x1;
-    carry_val[tile] = c;
+    carry_val[tile] = open ? run + w_cin[warp] : run;
   }
 }
 
@@ -230,8 +264,8 @@ bool dispatch_shape(const MpMatrix& m, const void* x, void* y, cudaStream_t s, c
 }  // namespace
 
 size_t mp_smem_bytes(const MpShape& sh, size_t value_bytes) {
-  size_t ipc = (size_t)sh.tpb * sh.ipt;
-  return 2 * ipc * value_bytes + (size_t)sh.tpb * value_bytes + ipc * sizeof(int) + (size_t)sh.tpb * sizeof(int);
+  const size_t ipc = (size_t)sh.tpb * sh.ipt, warps = (size_t)sh.tpb / 32;
+  return 2 * ipc * value_bytes + 2 * warps * value_bytes + ipc * sizeof(int) + warps * sizeof(int);
 }
 
 bool mp_partition(const MpMatrix& m, cudaStream_t s) {
