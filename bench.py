@@ -334,6 +334,45 @@ def form_legs(m, xv, B: int, flush, stream, steps: int, warmup: int) -> dict:
     return legs
 
 
+# Held-out records of the tuner's data set (never trained on): seeds 2000-2199
+# and the large records with (seed - 3000) % 4 == 3.
+TUNER_LIVE_SEEDS = (2003, 2026, 2049, 2072, 2095, 2118, 2141, 2164, 2187, 3003, 3007)
+
+
+def tuner_live_leg(seeds=TUNER_LIVE_SEEDS, reps: int = 3) -> dict:
+    """Regret of the learned selection measured live on this GPU: for held-out
+    matrices of the tuner's generator mix, the configuration the built-in model
+    picks against a fresh exhaustive autotune of every configuration."""
+    from vnec_gb300 import api
+    from vnec_gb300.tuner import dataset
+
+    rows, regrets, b_learned, b_best, t_learned, t_best = [], [], 0, 0, 0.0, 0.0
+    t0 = time.time()
+    for sd in seeds:
+        m, fam, desc = dataset.sample(sd)
+        choice, _, ood = api.learned_choice(m)
+        ms, best = api.autotune(m, reps=reps)
+        ok = np.isfinite(ms)
+        chosen_ms = float(ms[choice]) if ok[choice] else float("inf")
+        best_ms = float(np.min(ms[ok]))
+        r = chosen_ms / best_ms - 1.0
+        regrets.append(r)
+        bytes_ = dataset.algorithmic_bytes(m)
+        b_learned += bytes_
+        t_learned += chosen_ms
+        t_best += best_ms
+        rows.append({"seed": sd, "matrix": desc, "n_rows": m.n_rows, "nnz": m.nnz, "learned": int(choice),
+                     "best": int(best), "ms_learned": round(chosen_ms, 4), "ms_best": round(best_ms, 4),
+                     "regret": round(r, 4), "out_of_range": ood})
+        m.free()
+    return {"matrices": rows, "mean_regret": round(float(np.mean(regrets)), 4),
+            "max_regret": round(float(np.max(regrets)), 4),
+            "aggregate_gbs_learned": round(b_learned / t_learned / 1e6, 1),
+            "aggregate_gbs_exhaustive": round(b_learned / t_best / 1e6, 1),
+            "seconds": round(time.time() - t0, 1),
+            "how": f"exhaustive autotune ({reps} timed calls per configuration) on this GPU vs the model's choice"}
+
+
 def run_reference(args) -> None:
     ws, rank, _ = dist_env()
     if rank != 0:
@@ -406,7 +445,7 @@ def run_ours(args) -> None:
     prec = PRECISIONS[args.precision]
     if prec != api.PREC_FP64 and args.kernel != "S":
         raise SystemExit("--precision applies to the sliced kernel (--kernel S)")
-    plan = api.Plan(m, kernel=kernel, items_per_thread=-1 if args.kernel == "S" else 0, precision=prec,
+    plan = api.Plan(m, kernel=kernel, items_per_thread=args.unroll if args.kernel == "S" else 0, precision=prec,
                     shared_patterns=0 if args.shared_patterns == "on" else -1)
     t_plan = time.time() - t_plan
     info = plan.info()
@@ -547,6 +586,8 @@ def run_ours(args) -> None:
             legs["stencil256"] = form_legs(m2, x2, algorithmic_bytes(m2), flush, stream, args.leg_steps, args.warmup)
             m2.free()
         line["legs"] = legs
+        if args.workload == "rmat24":
+            line["tuner_live"] = tuner_live_leg()
         if args.workload == "rmat24" and not args.no_batch_leg:
             from vnec_gb300 import generators as G
 
@@ -802,6 +843,8 @@ def main() -> None:
                     help="sliced-kernel form of the main plan (the headline is fp64)")
     ap.add_argument("--shared-patterns", default="on", choices=["on", "off"],
                     help="precision forms: one copy of the column gaps for row groups that share them (default on)")
+    ap.add_argument("--unroll", type=int, default=-1, choices=[-1, 4, 8, 12, 16],
+                    help="sliced plans: loads in flight per lane (-1: timed on the matrix at plan build)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-legs", action="store_true", help="skip the precision-form / tuner / batch legs")
     ap.add_argument("--no-batch-leg", action="store_true", help="skip the batched-form legs of the default run")

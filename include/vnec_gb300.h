@@ -416,7 +416,9 @@ typedef struct {
                           the slots by shuffles; 0: tuned or normal */
   int host_parts;      /* host-vector calls run in this many parts so that X and Y copies overlap the
                           compute (0: 8, 1: one part) */
-  int reserved[5];
+  int dispatch;        /* 0: default, 1: persistent warps striding the task list, 2: one warp per task
+                          (blocks dispatched in task order, so the tasks in flight stay a compact window) */
+  int reserved[4];
 } SpB_VNEC_batch_options_ext;
 
 /* Plan from host CSR arrays per matrix: int64 row offsets (n_rows[m] + 1),

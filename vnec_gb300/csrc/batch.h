@@ -35,6 +35,7 @@ struct BatchMatrix {
   double* chunk_sum = nullptr;          // num_chunks * k partial sums
   int* chunk_count = nullptr;           // num_long arrival counters, 0 between calls
   int grid = 0;                         // persistent CTAs
+  bool per_task = false;                // one warp per task (blocks dispatched in task order) instead of persistent warps
   int warps_per_block = 8;
   int mode = 0;                         // 0: U steps in flight, 1: 2U, 2: entries staged in registers
   int precision = 0;                    // kPrecFP64, kPrecFP32 or kPrecDF32 (SlicedPrecision)

@@ -401,7 +401,16 @@ bool batch_spmm_range(const BatchMatrix& m, const double* X, double* Y, cudaStre
   a.klog2 = log2i(m.k);
   a.llog2 = log2i(m.lanes);
   void* fn = pick_kernel(m.precision, R, m.mode);
-  const int grid = (int)std::min<long long>(m.grid, std::max<long long>(1, (a.num_tasks + 7) / 8));
+  // Persistent warps stride the task list; with per_task every warp takes one
+  // task and the hardware dispatches the blocks in task order, so the tasks in
+  // flight stay a compact window of the list (and of X's rows).
+  const long long per_task_grid = (a.num_tasks + m.warps_per_block - 1) / m.warps_per_block;
+  if (m.per_task && per_task_grid > 0x7fffffffLL) {
+    set_error("batch: too many tasks for one launch with one warp per task");
+    return false;
+  }
+  const int grid = m.per_task ? (int)per_task_grid
+                              : (int)std::min<long long>(m.grid, std::max<long long>(1, (a.num_tasks + 7) / 8));
   void* args[] = {&a};
   return VNEC_CUDA(cudaLaunchKernel(fn, dim3((unsigned)grid), dim3((unsigned)(m.warps_per_block * 32)), args, 0, s));
 }

@@ -563,7 +563,8 @@ std::unique_ptr<Plan> build_batch(int n, const CsrView* mats, int k, const SpB_V
     set_error("batch: warps_per_block must be 4 or 8");
     return nullptr;
   }
-  if (o.long_row_len < 0 || o.chunk < 0 || o.window_rows < 0 || o.max_steps < 0 || o.unroll < 0 || o.unroll > 3) {
+  if (o.long_row_len < 0 || o.chunk < 0 || o.window_rows < 0 || o.max_steps < 0 || o.unroll < 0 || o.unroll > 3 ||
+      o.dispatch < 0 || o.dispatch > 2) {
     set_error("batch: negative option");
     return nullptr;
   }
@@ -652,6 +653,7 @@ std::unique_ptr<Plan> build_batch(int n, const CsrView* mats, int k, const SpB_V
     return nullptr;
   }
   const bool ok = upload_batch(h, k, o.precision, choice.wpb, choice.deep, &p->d);
+  p->d.m.per_task = o.dispatch == 2;
   if (ok) plan_parts(p.get(), batch_view(h), o.host_parts > 0 ? o.host_parts : 8);
   batch_free(h);
   if (!ok) return nullptr;

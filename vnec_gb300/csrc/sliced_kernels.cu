@@ -195,17 +195,14 @@ __device__ __forceinline__ V epi_out(V acc, int row, const SlicedEpilogue& ep) {
   }
 }
 
-template <typename V, int U, int H, bool HOT = false, bool EPI = false>
-__global__ void __launch_bounds__(kWarpsPerBlock * 32)
-sliced_kernel(const SlicedTask* __restrict__ tasks, long long num_tasks, const V* __restrict__ val,
-              const int32_t* __restrict__ col, const int32_t* __restrict__ rowid, const V* __restrict__ x,
-              V* y, V* __restrict__ chunk_sum, const int* __restrict__ guard = nullptr,
-              const V* __restrict__ xh = nullptr, int ncols = 0, SlicedEpilogue ep = SlicedEpilogue(),
-              const uint16_t* __restrict__ col16 = nullptr, const int32_t* __restrict__ first = nullptr) {
-  if (guard && *reinterpret_cast<const volatile int*>(guard) == 0) return;
-  const long long w = ((long long)blockIdx.x * kWarpsPerBlock) + (threadIdx.x >> 5);
-  const int lane = threadIdx.x & 31;
-  if (w >= num_tasks) return;
+// One warp task (the body of sliced_kernel and of the DF32 guard kernel).
+template <typename V, int U, int H, bool HOT, bool EPI>
+__device__ __forceinline__ void sliced_task(long long w, int lane, const SlicedTask* __restrict__ tasks,
+                                            const V* __restrict__ val, const int32_t* __restrict__ col,
+                                            const int32_t* __restrict__ rowid, const V* __restrict__ x, V* y,
+                                            V* __restrict__ chunk_sum, const V* __restrict__ xh, int ncols,
+                                            const SlicedEpilogue& ep, const uint16_t* __restrict__ col16,
+                                            const int32_t* __restrict__ first) {
   const int4 raw = __ldg(reinterpret_cast<const int4*>(tasks) + w);
   const int base = raw.x, row_base = raw.y, steps = raw.z, meta = raw.w;
   const int kind = meta & 15, vwl = (meta >> 4) & 15, nrows = (meta >> 8) & 0xff;
@@ -285,6 +282,37 @@ sliced_kernel(const SlicedTask* __restrict__ tasks, long long num_tasks, const V
   }
 }
 
+template <typename V, int U, int H, bool HOT = false, bool EPI = false>
+__global__ void __launch_bounds__(kWarpsPerBlock * 32)
+sliced_kernel(const SlicedTask* __restrict__ tasks, long long num_tasks, const V* __restrict__ val,
+              const int32_t* __restrict__ col, const int32_t* __restrict__ rowid, const V* __restrict__ x,
+              V* y, V* __restrict__ chunk_sum, const V* __restrict__ xh = nullptr, int ncols = 0,
+              SlicedEpilogue ep = SlicedEpilogue(), const uint16_t* __restrict__ col16 = nullptr,
+              const int32_t* __restrict__ first = nullptr) {
+  const long long w = ((long long)blockIdx.x * kWarpsPerBlock) + (threadIdx.x >> 5);
+  if (w >= num_tasks) return;
+  sliced_task<V, U, H, HOT, EPI>(w, threadIdx.x & 31, tasks, val, col, rowid, x, y, chunk_sum, xh, ncols, ep, col16,
+                                 first);
+}
+
+// FP64 recompute of a DF32 call whose x left the split range: a small grid of
+// warps striding the task list, so that the launch costs next to nothing in
+// the usual case (flag clear: every block returns at once).
+template <bool HOT>
+__global__ void __launch_bounds__(kWarpsPerBlock * 32)
+sliced_guard_kernel(const int* __restrict__ guard, const SlicedTask* __restrict__ tasks, long long num_tasks,
+                    const double* __restrict__ val, const int32_t* __restrict__ col,
+                    const int32_t* __restrict__ rowid, const double* __restrict__ x, double* y,
+                    double* __restrict__ chunk_sum, const double* __restrict__ xh, int ncols,
+                    const uint16_t* __restrict__ col16, const int32_t* __restrict__ first) {
+  if (*reinterpret_cast<const volatile int*>(guard) == 0) return;
+  const SlicedEpilogue ep;
+  const long long stride = (long long)gridDim.x * kWarpsPerBlock;
+  for (long long w = (long long)blockIdx.x * kWarpsPerBlock + (threadIdx.x >> 5); w < num_tasks; w += stride)
+    sliced_task<double, 8, 0, HOT, false>(w, threadIdx.x & 31, tasks, val, col, rowid, x, y, chunk_sum, xh, ncols,
+                                          ep, col16, first);
+}
+
 template <typename V, bool EPI = false>
 __global__ void sliced_long_fixup(const int32_t* __restrict__ long_row, const int32_t* __restrict__ long_first,
                                   long long num_long, const V* __restrict__ chunk_sum, V* y,
@@ -347,7 +375,7 @@ bool launch_main(const SlicedMatrix& m, const void* x, void* y, cudaStream_t s,
   }
   kern<<<(unsigned)grid, kWarpsPerBlock * 32, 0, s>>>(m.tasks, m.num_tasks, static_cast<const V*>(m.val), m.col,
                                                       m.rowid, static_cast<const V*>(x), static_cast<V*>(y),
-                                                      static_cast<V*>(m.chunk_sum), nullptr,
+                                                      static_cast<V*>(m.chunk_sum),
                                                       static_cast<const V*>(m.xhot), (int)m.n_cols, ep, m.col16,
                                                       m.first);
   return VNEC_CUDA(cudaGetLastError());
@@ -418,19 +446,22 @@ bool launch(const SlicedMatrix& m, const void* x, void* y, cudaStream_t s, cudaE
 bool sliced_guard_f64(const SlicedMatrix& m, const double* x, double* y, const int* flag, cudaStream_t s) {
   // The guard only runs for DF32 plans, whose FP64 values sit in m.val and
   // whose hot columns (if any) are served from x directly through hot_cols.
-  const long long grid = (m.num_tasks + kWarpsPerBlock - 1) / kWarpsPerBlock;
+  int dev = 0, sms = 0;
+  if (!VNEC_CUDA(cudaGetDevice(&dev)) || !VNEC_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)))
+    return false;
+  const long long need = (m.num_tasks + kWarpsPerBlock - 1) / kWarpsPerBlock;
+  const unsigned grid = (unsigned)std::max<long long>(1, std::min<long long>(need, 8LL * sms));
   if (m.hot > 0) {
     gather_hot<double><<<(unsigned)((m.hot + 255) / 256), 256, 0, s>>>(x, m.hot_cols, m.hot,
                                                                        static_cast<double*>(m.xhot));
     if (!VNEC_CUDA(cudaGetLastError())) return false;
-    sliced_kernel<double, 8, 0, true><<<(unsigned)grid, kWarpsPerBlock * 32, 0, s>>>(
-        m.tasks, m.num_tasks, static_cast<const double*>(m.val), m.col, m.rowid, x, y,
-        static_cast<double*>(m.chunk_sum), flag, static_cast<const double*>(m.xhot), (int)m.n_cols,
-        SlicedEpilogue(), m.col16, m.first);
+    sliced_guard_kernel<true><<<grid, kWarpsPerBlock * 32, 0, s>>>(
+        flag, m.tasks, m.num_tasks, static_cast<const double*>(m.val), m.col, m.rowid, x, y,
+        static_cast<double*>(m.chunk_sum), static_cast<const double*>(m.xhot), (int)m.n_cols, m.col16, m.first);
   } else {
-    sliced_kernel<double, 8, 0><<<(unsigned)grid, kWarpsPerBlock * 32, 0, s>>>(
-        m.tasks, m.num_tasks, static_cast<const double*>(m.val), m.col, m.rowid, x, y,
-        static_cast<double*>(m.chunk_sum), flag, nullptr, 0, SlicedEpilogue(), m.col16, m.first);
+    sliced_guard_kernel<false><<<grid, kWarpsPerBlock * 32, 0, s>>>(
+        flag, m.tasks, m.num_tasks, static_cast<const double*>(m.val), m.col, m.rowid, x, y,
+        static_cast<double*>(m.chunk_sum), nullptr, 0, m.col16, m.first);
   }
   return VNEC_CUDA(cudaGetLastError());
 }
