@@ -644,7 +644,8 @@ def batch_legs(mats, ks, precs, steps: int, warmup: int, dev, flush, stream, ws:
             t_plan = time.time()
             if tile:  # fixed layout (lanes, long-row limit, warps per block, unroll), no autotune
                 plan = api.BatchPlan(mats, k, precision=prec, lanes=tile[0], long_row_len=tile[1],
-                                     warps_per_block=tile[2], unroll=tile[3])
+                                     warps_per_block=tile[2], unroll=tile[3],
+                                     dispatch=tile[4] if len(tile) > 4 else 0)
             else:
                 plan = api.BatchPlan(mats, k, precision=prec, autotune=True)
             t_plan = time.time() - t_plan
@@ -834,7 +835,8 @@ def main() -> None:
     ap.add_argument("--batch-precision", default="fp64", help="batch512: fp64,fp32")
     ap.add_argument("--batch-mats", type=int, default=512)
     ap.add_argument("--batch-steps", type=int, default=10)
-    ap.add_argument("--batch-tile", default="", help="batch512: fixed lanes,long_row_len,warps_per_block,unroll "
+    ap.add_argument("--batch-tile", default="", help="batch512: fixed lanes,long_row_len,warps_per_block,unroll"
+                                                     "[,dispatch: 1 persistent warps, 2 one warp per task] "
                                                      "instead of the autotuner")
     ap.add_argument("--kernel", default="S", choices=["L", "S", "D"])
     ap.add_argument("--l2", default="flushed", choices=["flushed", "warm"],

@@ -311,3 +311,31 @@ def test_batch_config_scale_sample(built):
         check(p.mxv_host(X), Yref, cond, TOL[0])
     finally:
         p.free()
+
+
+@pytest.mark.parametrize("k", [1, 8, 32])
+@pytest.mark.parametrize("precision", [0, 1, 3], ids=["fp64", "fp32", "df32"])
+def test_batch_dispatch_modes_bit_identical(built, batch, k, precision):
+    """One warp per task (blocks dispatched in task order) and persistent warps
+    striding the task list run every task the same way: identical Y, also
+    through the host path split into parts and with the autotuner choosing."""
+    from vnec_gb300 import api
+
+    outs = []
+    for dispatch in (1, 2):
+        p = api.BatchPlan(batch, k, precision=precision, long_row_len=64, dispatch=dispatch)
+        try:
+            X = _x(p, k)
+            outs.append(p.mxv_host(X))
+            assert p.mxv_host(X).tobytes() == outs[-1].tobytes()
+        finally:
+            p.free()
+    assert outs[0].tobytes() == outs[1].tobytes()
+    p = api.BatchPlan(batch, k, precision=precision, autotune=True)
+    try:
+        ro, co = p.offsets()
+        X = _x(p, k)
+        Yref, cond = oracle_batch(batch, X, k, co, ro)
+        check(p.mxv_host(X), Yref, cond, TOL[precision])
+    finally:
+        p.free()
