@@ -352,6 +352,15 @@ SpB_Info SpB_VNEC_features_ext(int64_t n_rows, int64_t n_cols, const int64_t *ro
 int SpB_VNEC_autotune_ext(const SpB_VNEC_options_ext *base, SpB_Type type, int64_t n_rows, int64_t n_cols,
                           const int64_t *row_ptr, const int32_t *col, const void *val, int reps, float *ms);
 
+/* Times only the listed configurations, with the protocol of
+ * SpB_VNEC_autotune_ext (the median of `reps` calls, L2 flushed before
+ * each); ms[i] is the time of configs[i] (FLT_MAX where it cannot be built).
+ * Used to refresh stored timings of the configurations whose kernels changed.
+ * Returns 0, or -1 on invalid arguments. */
+int SpB_VNEC_time_configs_ext(const SpB_VNEC_options_ext *base, SpB_Type type, int64_t n_rows, int64_t n_cols,
+                              const int64_t *row_ptr, const int32_t *col, const void *val, int reps,
+                              const int *configs, int n_configs, float *ms);
+
 /* Configuration index the reference's rule and the built-in model choose
  * (the latter also writes the predicted relative costs, log2 units, and
  * whether a feature lies outside its training range).  -1 on failure or,

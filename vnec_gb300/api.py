@@ -166,6 +166,9 @@ def lib() -> C.CDLL:
     L.SpB_VNEC_autotune_ext.argtypes = [C.POINTER(Options), C.c_int, C.c_int64, C.c_int64, _vp, _vp, _vp, C.c_int,
                                         _vp]
     L.SpB_VNEC_autotune_ext.restype = C.c_int
+    L.SpB_VNEC_time_configs_ext.argtypes = [C.POINTER(Options), C.c_int, C.c_int64, C.c_int64, _vp, _vp, _vp,
+                                            C.c_int, _vp, C.c_int, _vp]
+    L.SpB_VNEC_time_configs_ext.restype = C.c_int
     L.SpB_VNEC_rule_choice_ext.argtypes = [C.c_int, C.c_int64, C.c_int64, _vp, _vp, _vp]
     L.SpB_VNEC_rule_choice_ext.restype = C.c_int
     L.SpB_VNEC_learned_choice_ext.argtypes = [C.c_int, C.c_int64, C.c_int64, _vp, _vp, _vp, _vp, _vp]
@@ -614,6 +617,21 @@ def autotune(csr, reps: int = 5, opts: Options | None = None) -> tuple[np.ndarra
     ms = ms.astype(np.float64)
     ms[ms >= np.finfo(np.float32).max] = np.inf
     return ms, best
+
+
+def time_configs(csr, configs, reps: int = 5, opts: Options | None = None) -> np.ndarray:
+    """Median ms of the listed configurations only (inf where unavailable), same protocol as `autotune`."""
+    rp, ci, vv = _csr_args(csr)
+    cfg = np.ascontiguousarray(configs, dtype=np.int32)
+    ms = np.zeros(len(cfg), dtype=np.float32)
+    o = opts or options()
+    rc = lib().SpB_VNEC_time_configs_ext(C.byref(o), SpB_FP64, csr.n_rows, csr.n_cols, rp.ctypes.data,
+                                         ci.ctypes.data, vv.ctypes.data, reps, cfg.ctypes.data, len(cfg),
+                                         ms.ctypes.data)
+    _check(rc == 0, "SpB_VNEC_time_configs_ext")
+    ms = ms.astype(np.float64)
+    ms[ms >= np.finfo(np.float32).max] = np.inf
+    return ms
 
 
 def rule_choice(csr) -> int:

@@ -118,7 +118,10 @@ bool config_available(int i, bool sorted_cols) {
 
 // Exhaustive search: every available configuration built and timed; ms[i] =
 // FLT_MAX for configurations that cannot be built.  Returns the fastest index.
-int autotune_search(const CsrView& v, const SpB_VNEC_options_ext* base, int reps, float* ms) {
+// Times every available configuration (only those with only[i] != 0 when
+// `only` is given); ms[i] = FLT_MAX for the rest.  Returns the fastest index.
+int autotune_search(const CsrView& v, const SpB_VNEC_options_ext* base, int reps, float* ms,
+                    const uint8_t* only = nullptr) {
   const bool sorted = cols_sorted(v);
   const size_t vb = v.value_bytes();
   DeviceBuffer dx, dy, flush;
@@ -137,6 +140,7 @@ int autotune_search(const CsrView& v, const SpB_VNEC_options_ext* base, int reps
   }
   for (int i = 0; i < kNumConfigs; ++i) {
     ms[i] = FLT_MAX;
+    if (only && !only[i]) continue;
     if (!available(i, v, sorted, base ? base->precision : 0)) continue;
     std::unique_ptr<Plan> p = build_config(i, v, base);
     if (!p) continue;
@@ -261,6 +265,31 @@ int SpB_VNEC_autotune_ext(const SpB_VNEC_options_ext* base, SpB_Type type, int64
   }
   if (!validate_csr(v, false)) return -1;
   return autotune_search(v, base, reps, ms);
+}
+
+int SpB_VNEC_time_configs_ext(const SpB_VNEC_options_ext* base, SpB_Type type, int64_t n_rows, int64_t n_cols,
+                              const int64_t* row_ptr, const int32_t* col, const void* val, int reps,
+                              const int* configs, int n_configs, float* ms) {
+  clear_error();
+  CsrView v;
+  if (!ms || !configs || n_configs < 1 || reps < 1 ||
+      !view_from_arrays(type, n_rows, n_cols, row_ptr, col, val, &v)) {
+    if (!ms || !configs || n_configs < 1 || reps < 1) set_error("SpB_VNEC_time_configs_ext: invalid arguments");
+    return -1;
+  }
+  if (!validate_csr(v, false)) return -1;
+  uint8_t only[kNumConfigs] = {0};
+  for (int i = 0; i < n_configs; ++i) {
+    if (configs[i] < 0 || configs[i] >= kNumConfigs) {
+      set_error("SpB_VNEC_time_configs_ext: configuration index out of range");
+      return -1;
+    }
+    only[configs[i]] = 1;
+  }
+  float all[kNumConfigs];
+  autotune_search(v, base, reps, all, only);
+  for (int i = 0; i < n_configs; ++i) ms[i] = all[configs[i]];
+  return 0;
 }
 
 int SpB_VNEC_rule_choice_ext(SpB_Type type, int64_t n_rows, int64_t n_cols, const int64_t* row_ptr,
