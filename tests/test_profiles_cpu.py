@@ -57,5 +57,4 @@ def test_bench_finds_the_summaries_it_reports():
     for form in ("fp32", "bf16", "df32"):
         # both layouts: the default shared-pattern tasks and per-lane deltas (--shared-patterns off)
         assert bench.profiled_traffic("sliced_mixed_kernel", f"stencil256_{form}_noshared") > 0
-    for form in ("fp32", "bf16"):
         assert bench.profiled_traffic("sliced_mixed_kernel", f"stencil256_{form}") > 0

@@ -168,7 +168,7 @@ struct TuneChoice {
   // warps striding the task list.  The default: on the 512-matrix batch it
   // keeps the tasks in flight, and so the rows of X they gather, a compact
   // window (k = 32: DF32 27.2 -> 17.6 ms, FP32 11.6 -> 8.2 ms, FP64 31.3 ->
-  // 29.4 ms per call).
+  // 29.4 ms per call).  The autotuner decides it on the whole batch.
   bool per_task = true;
 };
 
@@ -371,6 +371,35 @@ bool autotune(const BatchSource& s, int k, int precision, const SpB_VNEC_batch_o
     set_error("batch autotune: no candidate layout could be built");
     return false;
   }
+  return true;
+}
+
+// Times the uploaded plan with persistent warps and with one warp per task
+// (median of 3 calls after one warm-up each, on scratch X and Y) and keeps
+// persistent warps only when they win by more than 3 %.
+bool whole_batch_dispatch(BatchMatrix& m, int64_t n_rows, int64_t n_cols, int k, bool* per_task) {
+  TimingStream ts;
+  DeviceBuffer X, Y;
+  if (!ts.create()) {
+    set_error("batch dispatch timing: cannot create a stream or events");
+    return false;
+  }
+  const size_t nx = (size_t)std::max<int64_t>(n_cols, 1) * k, ny = (size_t)std::max<int64_t>(n_rows, 1) * k;
+  if (!X.alloc(nx * 8) || !Y.alloc(ny * 8) || !VNEC_CUDA(cudaMemset(X.ptr, 0x3f, nx * 8))) return false;
+  float med[2] = {0.f, 0.f};
+  for (int pt = 0; pt < 2; ++pt) {
+    m.per_task = pt != 0;
+    std::vector<float> t;
+    for (int rep = 0; rep < 4; ++rep) {
+      if (!VNEC_CUDA(cudaEventRecord(ts.e0, ts.s)) || !batch_spmm(m, X.as<double>(), Y.as<double>(), ts.s) ||
+          !VNEC_CUDA(cudaEventRecord(ts.e1, ts.s)) || !VNEC_CUDA(cudaEventSynchronize(ts.e1)))
+        return false;
+      float ms = 0.f;
+      if (rep >= 1 && VNEC_CUDA(cudaEventElapsedTime(&ms, ts.e0, ts.e1))) t.push_back(ms);
+    }
+    med[pt] = median_ms(t);
+  }
+  *per_task = !(med[0] < 0.97f * med[1]);
   return true;
 }
 
@@ -641,8 +670,10 @@ std::unique_ptr<Plan> build_batch(int n, const CsrView* mats, int k, const SpB_V
   if (o.long_row_len > 0) choice.long_len = o.long_row_len;
   if (o.warps_per_block > 0) choice.wpb = o.warps_per_block;
   if (o.unroll > 0) choice.deep = o.unroll - 1;
+  bool fresh = false;  // layout tuned here: the dispatch is then decided on the whole batch
+  std::string key;
   if (o.autotune) {
-    const std::string key = tune_key(src, k, o.precision);
+    key = tune_key(src, k, o.precision);
     bool hit = false;
     if (o.lanes == 0 && o.long_row_len == 0 && o.warps_per_block == 0 && o.unroll == 0 &&
         o.dispatch == 0) {
@@ -659,12 +690,7 @@ std::unique_ptr<Plan> build_batch(int n, const CsrView* mats, int k, const SpB_V
     if (!hit) {
       if (!autotune(src, k, o.precision, &o, &p->tuning)) return nullptr;
       choice = p->tuning.cand[(size_t)p->tuning.best];
-      if (o.lanes == 0 && o.long_row_len == 0 && o.warps_per_block == 0 && o.unroll == 0 &&
-          o.dispatch == 0) {
-        std::lock_guard<std::mutex> g(g_tune_mu);
-        tune_cache()[key] = choice;
-        cache_file_store(key, choice);
-      }
+      fresh = true;
     }
   }
   p->prm.lanes = choice.lanes;
@@ -680,6 +706,21 @@ std::unique_ptr<Plan> build_batch(int n, const CsrView* mats, int k, const SpB_V
     return nullptr;
   }
   const bool ok = upload_batch(h, k, o.precision, choice.wpb, choice.deep, &p->d);
+  if (ok && fresh && o.dispatch == 0) {
+    // The sample the layout was tuned on holds a fraction of the batch, so
+    // how far the persistent warps' drift spreads the rows of X they gather
+    // shows only on the whole batch: time both dispatches on it.
+    if (!whole_batch_dispatch(p->d.m, p->n_rows, p->n_cols, k, &choice.per_task)) {
+      batch_free(h);
+      return nullptr;
+    }
+  }
+  if (fresh && o.lanes == 0 && o.long_row_len == 0 && o.warps_per_block == 0 && o.unroll == 0 &&
+      o.dispatch == 0) {
+    std::lock_guard<std::mutex> g(g_tune_mu);
+    tune_cache()[key] = choice;
+    cache_file_store(key, choice);
+  }
   p->d.m.per_task = o.dispatch == 0 ? choice.per_task : o.dispatch == 2;
   if (ok) plan_parts(p.get(), batch_view(h), o.host_parts > 0 ? o.host_parts : 8);
   batch_free(h);
