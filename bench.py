@@ -334,6 +334,55 @@ def form_legs(m, xv, B: int, flush, stream, steps: int, warmup: int) -> dict:
     return legs
 
 
+def gather_ceiling_leg(m, x, flush, stream, spmv_ms: float, steps: int = 10) -> dict:
+    """The device's ceiling for a kernel that gathers x once per nonzero: the
+    measurement kernel (SpB_VNEC_stream_gather_ext: per item a coalesced
+    value and column read, one gather of x, one FP64 FMA, no row structure)
+    on this matrix's own column stream in CSR order and on uniform random
+    columns over windows of x of 1 MB, 16.8 MB and all of x; items per second
+    beside the SpMV kernel's nonzeros per second."""
+    import torch
+
+    from vnec_gb300 import api
+
+    dev = x.device
+    n = m.nnz
+    val = torch.from_numpy(np.ascontiguousarray(m.val[:n], dtype=np.float64)).to(dev)
+    out = torch.empty(api.STREAM_GATHER_BLOCKS, dtype=torch.float64, device=dev)
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(5)
+    res = {}
+    for name, w in (("matrix_csr_order", m.n_cols), ("uniform_window_1MB", 1 << 17),
+                    ("uniform_window_16.8MB", 1 << 21), ("uniform_all_of_x", m.n_cols)):
+        if name == "matrix_csr_order":
+            col = torch.from_numpy(np.ascontiguousarray(m.col[:n], dtype=np.int32)).to(dev)
+        else:
+            col = torch.randint(0, w, (n,), generator=gen, device=dev, dtype=torch.int32)
+        with torch.cuda.stream(stream):
+            for _ in range(3):
+                api.stream_gather(x.data_ptr(), m.n_cols, col.data_ptr(), val.data_ptr(), n, out.data_ptr(),
+                                  stream.cuda_stream)
+            ts = []
+            for i in range(steps):
+                flush.fill_(i)
+                a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                a.record(stream)
+                api.stream_gather(x.data_ptr(), m.n_cols, col.data_ptr(), val.data_ptr(), n, out.data_ptr(),
+                                  stream.cuda_stream)
+                b.record(stream)
+                b.synchronize()
+                ts.append(a.elapsed_time(b))
+        ms = float(np.median(ts))
+        res[name] = {"ms": round(ms, 5), "g_items_per_s": round(n / ms / 1e6, 1),
+                     "gbs_stream_and_window": round((12.0 * n + 8.0 * w) / ms / 1e6, 1)}
+        del col
+    res["spmv_kernel_g_nnz_per_s"] = round(n / spmv_ms / 1e6, 1)
+    res["spmv_vs_csr_order_ceiling"] = round(res["matrix_csr_order"]["ms"] / spmv_ms, 3)
+    res["how"] = ("SpB_VNEC_stream_gather_ext on the same nonzero count, L2 flushed before each call; the "
+                  "SpMV kernel also writes y and reads its task and row metadata")
+    return res
+
+
 # Held-out records of the tuner's data set (never trained on): seeds 2000-2199
 # and the large records with (seed - 3000) % 4 == 3.
 TUNER_LIVE_SEEDS = (2003, 2026, 2049, 2072, 2095, 2118, 2141, 2164, 2187, 3003, 3007)
@@ -588,6 +637,8 @@ def run_ours(args) -> None:
         line["legs"] = legs
         if args.workload == "rmat24":
             line["tuner_live"] = tuner_live_leg()
+        if args.workload in ("rmat24", "rmat22"):
+            line["gather_ceiling"] = gather_ceiling_leg(m, x, flush, stream, float(np.mean(main_ms)))
         if args.workload == "rmat24" and not args.no_batch_leg:
             from vnec_gb300 import generators as G
 

@@ -286,6 +286,18 @@ SpB_Info SpB_VNEC_wait_polls_ext(void *plan, int64_t polls);
  * the FP32/BF16 precision forms, exposed for callers keeping x in FP32. */
 SpB_Info SpB_VNEC_f64_to_f32_ext(const double *d_in, float *d_out, int64_t n, void *stream);
 
+/* Measurement kernel (no counterpart in the reference; no SpMV path uses it).
+ * For i in [0, n) it reads d_val[i] and d_col[i] with coalesced loads,
+ * gathers d_x[d_col[i]] (columns must lie in [0, n_x)) and accumulates the
+ * FP64 product: the memory traffic of n CSR nonzeros without the row
+ * structure.  d_out receives SPB_VNEC_STREAM_GATHER_BLOCKS partial sums.
+ * Its rate on a matrix's own column stream, and on uniform random columns
+ * over windows of chosen size, is the device's ceiling for kernels that
+ * gather x once per nonzero (bench.py reports it beside the SpMV). */
+#define SPB_VNEC_STREAM_GATHER_BLOCKS 4096
+SpB_Info SpB_VNEC_stream_gather_ext(const double *d_x, int64_t n_x, const int32_t *d_col, const double *d_val,
+                                    int64_t n, double *d_out, void *stream);
+
 /* Allocation-free y := A x (no counterpart in the reference).
  *
  * For callers that cannot let a library allocate device memory: hosts whose

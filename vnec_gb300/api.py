@@ -169,6 +169,8 @@ def lib() -> C.CDLL:
     L.SpB_VNEC_time_configs_ext.argtypes = [C.POINTER(Options), C.c_int, C.c_int64, C.c_int64, _vp, _vp, _vp,
                                             C.c_int, _vp, C.c_int, _vp]
     L.SpB_VNEC_time_configs_ext.restype = C.c_int
+    L.SpB_VNEC_stream_gather_ext.argtypes = [_vp, C.c_int64, _vp, _vp, C.c_int64, _vp, _vp]
+    L.SpB_VNEC_stream_gather_ext.restype = C.c_int
     L.SpB_VNEC_rule_choice_ext.argtypes = [C.c_int, C.c_int64, C.c_int64, _vp, _vp, _vp]
     L.SpB_VNEC_rule_choice_ext.restype = C.c_int
     L.SpB_VNEC_learned_choice_ext.argtypes = [C.c_int, C.c_int64, C.c_int64, _vp, _vp, _vp, _vp, _vp]
@@ -632,6 +634,16 @@ def time_configs(csr, configs, reps: int = 5, opts: Options | None = None) -> np
     ms = ms.astype(np.float64)
     ms[ms >= np.finfo(np.float32).max] = np.inf
     return ms
+
+
+STREAM_GATHER_BLOCKS = 4096  # SPB_VNEC_STREAM_GATHER_BLOCKS
+
+
+def stream_gather(d_x: int, n_x: int, d_col: int, d_val: int, n: int, d_out: int, stream: int = 0) -> None:
+    """The measurement kernel: sum of val[i] * x[col[i]] over n items, as
+    STREAM_GATHER_BLOCKS partial sums in d_out (device pointers)."""
+    _check(lib().SpB_VNEC_stream_gather_ext(d_x, n_x, d_col, d_val, n, d_out, stream or None) == SpB_SUCCESS,
+           "SpB_VNEC_stream_gather_ext")
 
 
 def rule_choice(csr) -> int:
