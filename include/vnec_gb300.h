@@ -228,6 +228,23 @@ SpB_Info SpB_mxv_device_ext(void *plan, const void *d_x, void *d_y, void *stream
 SpB_Info SpB_mxv_axpby_ext(void *plan, const void *d_x, void *d_y, double alpha, double beta, const void *d_z,
                            double gamma, void *stream);
 
+/* As SpB_mxv_axpby_ext with one more additive term read on the device:
+ * y := alpha * (A x) + beta * z + gamma + g_scale * (*d_g), where d_g points
+ * to one double in device memory written by an earlier launch on the stream
+ * (for example SpB_VNEC_dot_ext), so a power iteration needs no host round
+ * trip for a data-dependent shift.  g_scale == 0 ignores d_g. */
+SpB_Info SpB_mxv_axpbyg_ext(void *plan, const void *d_x, void *d_y, double alpha, double beta, const void *d_z,
+                            double gamma, const double *d_g, double g_scale, void *stream);
+
+/* Deterministic device reduction over n FP64 values, for chains of calls that
+ * stay on the GPU: mode 0 writes sum_i a[i] * b[i], mode 1 sum_i |a[i] - b[i]|
+ * to d_out[0].  d_partial holds SPB_VNEC_DOT_BLOCKS doubles of scratch owned
+ * by the caller; the sum runs in a fixed order (identical bits run to run).
+ * Enqueued on `stream`. */
+#define SPB_VNEC_DOT_BLOCKS 1024
+SpB_Info SpB_VNEC_dot_ext(int64_t n, const double *d_a, const double *d_b, int mode, double *d_partial,
+                          double *d_out, void *stream);
+
 /* y := A x with host x and y (the SpB_mxv data path without SpB_Vector). */
 SpB_Info SpB_mxv_host_ext(void *plan, const void *h_x, void *h_y);
 

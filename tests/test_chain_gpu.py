@@ -77,3 +77,58 @@ def test_pagerank_chain(built, kernel):
     assert delta < 1e-13 and iters < 200
     assert abs(ranks.sum() - 1.0) < 1e-12
     assert np.abs(ranks - ref).sum() < 1e-11
+
+
+@pytest.mark.parametrize("n", [0, 1, 777, 1 << 20, (1 << 21) + 5])
+def test_device_dot_and_l1_distance(built, n):
+    """SpB_VNEC_dot_ext: sum a*b and sum |a - b| in a fixed order (identical
+    bits on repeated calls), within 1e-12 of the sums' magnitudes."""
+    import torch
+
+    from vnec_gb300 import api
+
+    rng = np.random.default_rng(n)
+    a, b = rng.uniform(-1, 1, n), rng.uniform(-1, 1, n)
+    da, db = torch.from_numpy(a).cuda(), torch.from_numpy(b).cuda()
+    part = torch.empty(api.DOT_BLOCKS, dtype=torch.float64, device="cuda")
+    out = torch.full((2,), float("nan"), dtype=torch.float64, device="cuda")
+    for mode, want, scale in ((0, float(np.dot(a, b)), float(np.abs(a * b).sum())),
+                              (1, float(np.abs(a - b).sum()), float(np.abs(a - b).sum()))):
+        got = []
+        for _ in range(2):
+            api.dot(n, da.data_ptr(), db.data_ptr(), mode, part.data_ptr(), out.data_ptr() + 8 * mode)
+            torch.cuda.synchronize()
+            got.append(float(out[mode].item()))
+        assert got[0] == got[1]
+        assert abs(got[0] - want) <= 1e-12 * scale + 1e-300
+
+
+@pytest.mark.parametrize("kernel", ["L", "S", "S_FP32FORM", "HYBRID"])
+def test_axpby_with_device_scalar(built, kernel):
+    """SpB_mxv_axpbyg_ext: y = alpha A x + beta z + gamma + s * (*d_g), the
+    scalar read on the device, fused or as the elementwise pass."""
+    import torch
+
+    from oracle import oracle as O
+    from vnec_gb300 import api
+    from vnec_gb300 import generators as G
+
+    kw = dict(kernel=api.KERNEL_S, precision=api.PREC_FP32) if kernel == "S_FP32FORM" else dict(
+        kernel=getattr(api, "KERNEL_" + kernel))
+    tol = 1e-6 if kernel == "S_FP32FORM" else 1e-12
+    m = G.rmat(14, 8 << 14, seed=4)
+    rng = np.random.default_rng(5)
+    xv, zv = rng.uniform(-1, 1, m.n_cols), rng.uniform(-1, 1, m.n_rows)
+    ax, cond = O.spmv_neumaier(m, xv)
+    p = api.Plan(m, long_row_len=64, **kw)
+    try:
+        x, z = torch.from_numpy(xv).cuda(), torch.from_numpy(zv).cuda()
+        g = torch.tensor([0.375], dtype=torch.float64, device="cuda")
+        y = torch.full((m.n_rows,), float("nan"), dtype=torch.float64, device="cuda")
+        p.mxv_axpbyg(x.data_ptr(), y.data_ptr(), 0.85, -0.5, z.data_ptr(), 0.1, g.data_ptr(), 2.0)
+        torch.cuda.synchronize()
+        want = 0.85 * ax - 0.5 * zv + 0.1 + 2.0 * 0.375
+        bound = tol * (0.85 * cond + 0.5 * np.abs(zv) + 0.85) + 1e-15
+        assert np.all(np.abs(y.cpu().numpy() - want) <= bound)
+    finally:
+        p.free()

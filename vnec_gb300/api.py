@@ -171,6 +171,10 @@ def lib() -> C.CDLL:
     L.SpB_VNEC_time_configs_ext.restype = C.c_int
     L.SpB_VNEC_stream_gather_ext.argtypes = [_vp, C.c_int64, _vp, _vp, C.c_int64, _vp, _vp]
     L.SpB_VNEC_stream_gather_ext.restype = C.c_int
+    L.SpB_mxv_axpbyg_ext.argtypes = [_vp, _vp, _vp, C.c_double, C.c_double, _vp, C.c_double, _vp, C.c_double, _vp]
+    L.SpB_mxv_axpbyg_ext.restype = C.c_int
+    L.SpB_VNEC_dot_ext.argtypes = [C.c_int64, _vp, _vp, C.c_int, _vp, _vp, _vp]
+    L.SpB_VNEC_dot_ext.restype = C.c_int
     L.SpB_VNEC_rule_choice_ext.argtypes = [C.c_int, C.c_int64, C.c_int64, _vp, _vp, _vp]
     L.SpB_VNEC_rule_choice_ext.restype = C.c_int
     L.SpB_VNEC_learned_choice_ext.argtypes = [C.c_int, C.c_int64, C.c_int64, _vp, _vp, _vp, _vp, _vp]
@@ -419,6 +423,12 @@ class Plan:
         _check(lib().SpB_mxv_axpby_ext(self.h, d_x, d_y, alpha, beta, d_z or None, gamma, stream or None)
                == SpB_SUCCESS, "SpB_mxv_axpby_ext")
 
+    def mxv_axpbyg(self, d_x: int, d_y: int, alpha: float = 1.0, beta: float = 0.0, d_z: int = 0,
+                   gamma: float = 0.0, d_g: int = 0, g_scale: float = 0.0, stream: int = 0) -> None:
+        """y = alpha * A x + beta * z + gamma + g_scale * (*d_g), d_g a device double."""
+        _check(lib().SpB_mxv_axpbyg_ext(self.h, d_x, d_y, alpha, beta, d_z or None, gamma, d_g or None, g_scale,
+                                        stream or None) == SpB_SUCCESS, "SpB_mxv_axpbyg_ext")
+
     def _host_sizes(self) -> tuple[int, int]:
         """Values of x and of y one host-vector call copies (n_cols and n_rows
         times the right-hand sides)."""
@@ -634,6 +644,16 @@ def time_configs(csr, configs, reps: int = 5, opts: Options | None = None) -> np
     ms = ms.astype(np.float64)
     ms[ms >= np.finfo(np.float32).max] = np.inf
     return ms
+
+
+DOT_BLOCKS = 1024  # SPB_VNEC_DOT_BLOCKS
+
+
+def dot(n: int, d_a: int, d_b: int, mode: int, d_partial: int, d_out: int, stream: int = 0) -> None:
+    """d_out[0] = sum a*b (mode 0) or sum |a - b| (mode 1) over n device doubles,
+    in a fixed order; d_partial holds DOT_BLOCKS doubles of scratch."""
+    _check(lib().SpB_VNEC_dot_ext(n, d_a, d_b, mode, d_partial, d_out, stream or None) == SpB_SUCCESS,
+           "SpB_VNEC_dot_ext")
 
 
 STREAM_GATHER_BLOCKS = 4096  # SPB_VNEC_STREAM_GATHER_BLOCKS

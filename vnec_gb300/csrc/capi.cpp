@@ -546,6 +546,32 @@ SpB_Info SpB_mxv_axpby_ext(void* plan, const void* d_x, void* d_y, double alpha,
   return p->run_epilogue(d_x, d_y, e, static_cast<cudaStream_t>(stream)) ? SpB_SUCCESS : SpB_FAILURE;
 }
 
+SpB_Info SpB_mxv_axpbyg_ext(void* plan, const void* d_x, void* d_y, double alpha, double beta, const void* d_z,
+                            double gamma, const double* d_g, double g_scale, void* stream) {
+  clear_error();
+  Plan* p = find_plan(plan);
+  if (!p) {
+    set_error("unknown plan");
+    return SpB_FAILURE;
+  }
+  if ((p->n_cols > 0 && !d_x) || (p->n_rows > 0 && !d_y)) {
+    set_error("x or y is NULL");
+    return SpB_FAILURE;
+  }
+  SlicedEpilogue e;
+  e.alpha = alpha;
+  e.beta = beta;
+  e.gamma = gamma;
+  e.z = beta != 0.0 ? d_z : nullptr;
+  e.gamma_dev = g_scale != 0.0 ? d_g : nullptr;
+  e.gamma_dev_scale = g_scale;
+  if (g_scale != 0.0 && !d_g) {
+    set_error("d_g is NULL");
+    return SpB_FAILURE;
+  }
+  return p->run_epilogue(d_x, d_y, e, static_cast<cudaStream_t>(stream)) ? SpB_SUCCESS : SpB_FAILURE;
+}
+
 SpB_Info SpB_mxv_host_ext(void* plan, const void* h_x, void* h_y) {
   clear_error();
   Plan* p = find_plan(plan);

@@ -119,6 +119,10 @@ SlicedHostView sliced_view(const SlicedHost* h);
 struct SlicedEpilogue {
   double alpha = 1.0, beta = 0.0, gamma = 0.0;
   const void* z = nullptr;
+  // Optional device scalar: gamma + gamma_dev_scale * *gamma_dev, read by the
+  // kernel (a value an earlier launch on the stream computed).
+  const double* gamma_dev = nullptr;
+  double gamma_dev_scale = 0.0;
 };
 
 bool sliced_spmv(const SlicedMatrix& m, bool fp64, const void* x, void* y, cudaStream_t s,

@@ -187,7 +187,8 @@ __device__ __forceinline__ const V* x_at(const V* __restrict__ x, const V* __res
 template <bool EPI, typename V>
 __device__ __forceinline__ V epi_out(V acc, int row, const SlicedEpilogue& ep) {
   if constexpr (EPI) {
-    double r = fma(ep.alpha, static_cast<double>(acc), ep.gamma);
+    const double g = ep.gamma_dev ? fma(ep.gamma_dev_scale, *ep.gamma_dev, ep.gamma) : ep.gamma;
+    double r = fma(ep.alpha, static_cast<double>(acc), g);
     if (ep.z) r = fma(ep.beta, static_cast<double>(static_cast<const V*>(ep.z)[row]), r);
     return static_cast<V>(r);
   } else {
@@ -328,7 +329,8 @@ __global__ void sliced_long_fixup(const int32_t* __restrict__ long_row, const in
 template <typename V>
 __global__ void epilogue_kernel(V* y, long long n, SlicedEpilogue ep) {
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-    double r = fma(ep.alpha, static_cast<double>(y[i]), ep.gamma);
+    const double g = ep.gamma_dev ? fma(ep.gamma_dev_scale, *ep.gamma_dev, ep.gamma) : ep.gamma;
+    double r = fma(ep.alpha, static_cast<double>(y[i]), g);
     if (ep.z) r = fma(ep.beta, static_cast<double>(static_cast<const V*>(ep.z)[i]), r);
     y[i] = static_cast<V>(r);
   }

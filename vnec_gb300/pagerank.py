@@ -8,9 +8,13 @@ runs as a chain of SpMV calls whose vectors never leave the GPU:
 
 with P the column-stochastic transition matrix of the graph (P[j, i] =
 1 / outdeg(i) for an edge i -> j).  P r is planned as the transpose of the
-row-scaled adjacency (``transpose=True``), and the scale by d plus the
-teleport term are fused into the SpMV's stores (``SpB_mxv_axpby_ext``); the
-dangling-mass correction and the convergence test are device reductions.
+row-scaled adjacency (``transpose=True``).  Every iteration runs only the
+library's kernels: a device dot product of r with the dangling mask
+(``SpB_VNEC_dot_ext``) writes the dangling mass to a device scalar, and the
+SpMV folds d, the teleport term and that scalar into its stores
+(``SpB_mxv_axpbyg_ext``).  Every ``check_every`` iterations a device L1
+distance (``SpB_VNEC_dot_ext``, mode 1) is read back for the convergence
+test: the only host round trip.
 """
 from __future__ import annotations
 
@@ -48,15 +52,19 @@ def pagerank(adj, d: float = 0.85, tol: float = 1e-12, max_iter: int = 200, kern
     dmask = torch.from_numpy(dangling.astype(np.float64)).to(dev)
     r = torch.full((n,), 1.0 / n, dtype=torch.float64, device=dev)
     y = torch.empty_like(r)
+    scal = torch.zeros(2, dtype=torch.float64, device=dev)  # [dangling mass, L1 distance]
+    part = torch.empty(api.DOT_BLOCKS, dtype=torch.float64, device=dev)
     stream = torch.cuda.current_stream(dev).cuda_stream
     delta = float("inf")
     it = 0
     try:
         for it in range(1, max_iter + 1):
-            plan.mxv_axpby(r.data_ptr(), y.data_ptr(), alpha=d, gamma=(1.0 - d) / n, stream=stream)
-            y.add_(torch.dot(r, dmask) * (d / n))
+            api.dot(n, r.data_ptr(), dmask.data_ptr(), 0, part.data_ptr(), scal.data_ptr(), stream)
+            plan.mxv_axpbyg(r.data_ptr(), y.data_ptr(), alpha=d, gamma=(1.0 - d) / n, d_g=scal.data_ptr(),
+                            g_scale=d / n, stream=stream)
             if it % check_every == 0 or it == max_iter:
-                delta = float(torch.sum(torch.abs(y - r)))
+                api.dot(n, y.data_ptr(), r.data_ptr(), 1, part.data_ptr(), scal.data_ptr() + 8, stream)
+                delta = float(scal[1].item())
                 r, y = y, r
                 if delta < tol:
                     break
