@@ -151,7 +151,8 @@ typedef struct {
   int kernel;            /* SpB_VNEC_kernel_ext */
   int threads_per_block; /* 0: default */
   int items_per_thread;  /* 0: default; sliced plans: load steps in flight 4/8/12/16,
-                            -1: timed on the matrix at plan build */
+                            0 or -1: each timed on the matrix at plan build (y is
+                            the same at every value) */
   int pipeline_stages;   /* merge-path: 0 default (2), 1 unpipelined kernel, 2-3 stages */
   int arithmetic;        /* SpB_VNEC_arith_ext (FP64 values) */
   int window_rows;       /* sliced: rows sorted within windows of this size (0: 65536) */
@@ -174,8 +175,9 @@ typedef struct {
                             is used, -1: off) */
   int lane_vectors;      /* sliced FP32 / BF16 forms: each lane's entries stored in runs of 4 /
                             8 consecutive steps, read as 16-byte vectors (0: where most
-                            entries use 16-bit column deltas, 1: on, -1: off; the sums
-                            are the same either way) */
+                            entries use 16-bit column deltas, except FP32 plans whose
+                            entries sit mostly in shared-pattern tasks; 1: on, -1: off;
+                            the sums are the same either way) */
   int hot_order;         /* sliced plans with a hot-column window: 0 (default) stores each
                             row's hot-window entries first, hottest first, and groups rows
                             of equal length by their hottest column, so the lanes of one

@@ -403,6 +403,16 @@ bool launch_unroll(const SlicedMatrix& m, const void* x, void* y, cudaStream_t s
   }
 }
 
+template <typename V, bool HOT>
+bool launch_fused(const SlicedMatrix& m, const void* x, void* y, cudaStream_t s, const SlicedEpilogue& ep) {
+  switch (m.unroll) {
+    case 4: return launch_main<V, 4, 0, HOT, true>(m, x, y, s, ep);
+    case 8: return launch_main<V, 8, 0, HOT, true>(m, x, y, s, ep);
+    case 16: return launch_main<V, 16, 0, HOT, true>(m, x, y, s, ep);
+    default: return launch_main<V, 12, 0, HOT, true>(m, x, y, s, ep);
+  }
+}
+
 template <typename V>
 bool launch_variant(const SlicedMatrix& m, const void* x, void* y, cudaStream_t s) {
   return m.hot > 0 ? launch_unroll<V, true>(m, x, y, s) : launch_unroll<V, false>(m, x, y, s);
@@ -412,16 +422,15 @@ template <typename V>
 bool launch(const SlicedMatrix& m, const void* x, void* y, cudaStream_t s, cudaEvent_t* ev,
             const SlicedEpilogue* epi) {
   if (ev && !VNEC_CUDA(cudaEventRecord(ev[0], s))) return false;
-  // The fused epilogue runs in the default variant (unroll 12, default cache
-  // hints); dense-block plans apply it as a separate pass.
+  // The fused epilogue runs at the plan's unroll with default cache hints;
+  // dense-block plans apply it as a separate pass.
   const bool fused = epi && m.vpe == 1;
   if (m.num_tasks > 0) {
     bool ok;
     if (m.vpe == 4)
       ok = launch_dense<V>(m, x, y, s);
     else if (fused)
-      ok = m.hot > 0 ? launch_main<V, 12, 0, true, true>(m, x, y, s, *epi)
-                     : launch_main<V, 12, 0, false, true>(m, x, y, s, *epi);
+      ok = m.hot > 0 ? launch_fused<V, true>(m, x, y, s, *epi) : launch_fused<V, false>(m, x, y, s, *epi);
     else
       ok = launch_variant<V>(m, x, y, s);
     if (!ok) return false;

@@ -376,7 +376,10 @@ std::unique_ptr<Plan> upload(std::unique_ptr<SlicedPlan> p, SlicedHost* h, int v
   // FP32 / BF16 forms: lane runs of 16 bytes of values (4 / 8 steps).  By
   // default where most entries sit in 16-bit-delta tasks (local columns,
   // stream-bound: the 256^3 stencil runs 11% / 7% faster); gather-bound
-  // layouts keep stride 32.
+  // layouts keep stride 32.  The FP32 form also keeps stride 32 where most
+  // entries sit in shared-pattern tasks: there its kernel needs 32 registers
+  // against 48 for lane runs, and the extra resident warps hide more latency
+  // than the 16-byte loads save (256^3 stencil, unroll 4: 0.560 -> 0.551 ms).
   std::vector<int32_t> col_runs;
   std::vector<uint16_t> col16_runs;
   const int32_t* cols = hv.col;
@@ -384,15 +387,17 @@ std::unique_ptr<Plan> upload(std::unique_ptr<SlicedPlan> p, SlicedHost* h, int v
   int run = 0;
   const int lv = opts ? opts->lane_vectors : 0;
   if ((prec == kPrecFP32 || prec == kPrecBF16) && hv.vpe == 1 && lv >= 0) {
-    int64_t delta_entries = 0;
+    int64_t delta_entries = 0, shared_entries = 0;
     bool aligned = true;
     for (int64_t t = 0; t < hv.num_tasks; ++t) {
       const SlicedTask& k = hv.tasks[t];
       if ((k.meta & 15) == kSlicedZero) continue;
       if (k.meta & kSlicedDelta) delta_entries += (int64_t)k.steps * 32;
+      if (k.meta & kSlicedShared) shared_entries += (int64_t)k.steps * 32;
       if (k.base % 32 != 0) aligned = false;  // vector loads need bases aligned to 32 entries
     }
-    if (aligned && (lv > 0 || 2 * delta_entries >= hv.entries)) run = prec == kPrecFP32 ? 4 : 8;
+    const bool fp32_shared = prec == kPrecFP32 && 2 * shared_entries >= hv.entries;
+    if (aligned && (lv > 0 || (2 * delta_entries >= hv.entries && !fp32_shared))) run = prec == kPrecFP32 ? 4 : 8;
   }
   if (run) {
     const size_t ne = (size_t)(hv.entries + pad);
@@ -489,12 +494,15 @@ std::unique_ptr<Plan> upload(std::unique_ptr<SlicedPlan> p, SlicedHost* h, int v
   p->delta_rows = hv.col16 ? hv.delta_rows : 0;
   // Options: cache_hints 2 explicit L1/L2 policies, 3 no L1 allocation for the
   // streamed arrays, 4 the same with L1 evict-last x gathers; items_per_thread
-  // selects the unroll (4, 8, 12, 16; default 12, the fastest of the four on
-  // R-MAT 2^24 and the 256^3 stencil in FP64).
+  // selects the unroll (4, 8, 12, 16), and by default (0 or -1) the plan times
+  // the four on the matrix: no one value suits every layout (R-MAT 2^24 runs
+  // fastest at 12, the 256^3 stencil's shared-pattern tasks at 4, where 12 is
+  // 1.4x slower in FP64).  The unroll changes how many loads are in flight,
+  // not the order of any row's sums: y is the same at every value.
   m.cache_hints = (opts && opts->cache_hints >= 2 && opts->cache_hints <= 4) ? opts->cache_hints - 1 : 0;
   const int ipt = opts ? opts->items_per_thread : 0;
   m.unroll = (ipt == 4 || ipt == 8 || ipt == 12 || ipt == 16) ? ipt : 12;
-  if (ipt == -1 && m.vpe == 1 && !p->tune_unroll()) return nullptr;
+  if ((ipt == 0 || ipt == -1) && m.vpe == 1 && !p->tune_unroll()) return nullptr;
   // Parts for host-vector calls: about 8 groups of whole windows with equal
   // entries (only plans that compute every row: no keep mask).
   const int kParts = (opts && opts->host_parts > 0) ? std::min(opts->host_parts, 1024) : 8;
