@@ -33,6 +33,15 @@ struct SlicedTask {
   int32_t meta;      // kind | vw_log2 << 4 | nrows << 8
 };
 
+// The long-row fix-up sums a row of at most this many chunks in one thread
+// and a longer row with a whole warp.
+constexpr int kHeavyChunks = 16;
+// Blocks of `threads` for the fix-up launch: one thread per long row, then
+// one warp per heavy row.
+struct FixupGrid {
+  unsigned light, total;
+};
+
 struct SlicedMatrix {
   int64_t n_rows = 0, n_cols = 0, nnz = 0, entries = 0;  // entries include padding
   int64_t num_tasks = 0, num_long = 0, num_chunks = 0;
@@ -42,6 +51,10 @@ struct SlicedMatrix {
   const int32_t* rowid = nullptr;   // group row slots
   const int32_t* long_row = nullptr;    // num_long rows
   const int32_t* long_first = nullptr;  // num_long + 1 chunk offsets
+  // Long rows of more than kHeavyChunks chunks (indices into long_row, minus
+  // heavy_sub): the fix-up sums each with a warp instead of one thread.
+  const int32_t* long_heavy = nullptr;
+  int64_t num_heavy = 0, heavy_sub = 0;
   void* chunk_sum = nullptr;            // num_chunks scratch (value type)
   int cache_hints = 0;                  // load cache-hint variant (sliced_kernels.cu), 0 default
   int unroll = 8;                       // load steps in flight per lane: 4, 8, 12 or 16
@@ -155,6 +168,11 @@ bool split_to_df32(const double* x, float2* xs, long long n, int* flag, cudaStre
 inline int sliced_mixed_launches(const SlicedMatrix& m, int precision) {
   return 2 + (precision == kPrecDF32 ? 1 : 0) + (m.num_long > 0 || precision == kPrecDF32 ? 1 : 0) +
          (precision == kPrecDF32 && m.hot > 0 ? 1 : 0);
+}
+inline FixupGrid fixup_grid(const SlicedMatrix& m, int threads) {
+  const int64_t light = (m.num_long + threads - 1) / threads;
+  const int64_t heavy = (m.num_heavy * 32 + threads - 1) / threads;
+  return FixupGrid{(unsigned)light, (unsigned)(light + heavy)};
 }
 inline int sliced_launches(const SlicedMatrix& m) { return (m.num_long > 0 ? 2 : 1) + (m.hot > 0 ? 1 : 0); }
 

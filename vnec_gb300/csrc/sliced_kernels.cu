@@ -17,6 +17,7 @@
 #include <cstdint>
 
 #include "common.h"
+#include "long_rows.cuh"
 #include "sliced.h"
 
 namespace vnec {
@@ -316,14 +317,14 @@ sliced_guard_kernel(const int* __restrict__ guard, const SlicedTask* __restrict_
 
 template <typename V, bool EPI = false>
 __global__ void sliced_long_fixup(const int32_t* __restrict__ long_row, const int32_t* __restrict__ long_first,
-                                  long long num_long, const V* __restrict__ chunk_sum, V* y,
+                                  const int32_t* __restrict__ long_heavy, long long num_long, long long num_heavy,
+                                  long long heavy_sub, unsigned light_blocks, const V* __restrict__ chunk_sum, V* y,
                                   SlicedEpilogue ep = SlicedEpilogue()) {
-  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= num_long) return;
-  V s = V(0);
-  for (int c = long_first[i]; c < long_first[i + 1]; ++c) s += chunk_sum[c];
-  const int row = long_row[i];
-  y[row] = epi_out<EPI>(s, row, ep);
+  long_rows_fixup<V>(long_first, long_heavy, num_long, num_heavy, heavy_sub, light_blocks, chunk_sum,
+                     [&](long long i, V s) {
+                       const int row = long_row[i];
+                       y[row] = epi_out<EPI>(s, row, ep);
+                     });
 }
 
 template <typename V>
@@ -438,13 +439,15 @@ bool launch(const SlicedMatrix& m, const void* x, void* y, cudaStream_t s, cudaE
   if (ev && !VNEC_CUDA(cudaEventRecord(ev[1], s))) return false;
   if (m.num_long > 0) {
     const int b = 128;
-    const unsigned g = (unsigned)((m.num_long + b - 1) / b);
+    const FixupGrid g = fixup_grid(m, b);
     if (fused)
-      sliced_long_fixup<V, true><<<g, b, 0, s>>>(m.long_row, m.long_first, m.num_long,
-                                                 static_cast<const V*>(m.chunk_sum), static_cast<V*>(y), *epi);
+      sliced_long_fixup<V, true><<<g.total, b, 0, s>>>(m.long_row, m.long_first, m.long_heavy, m.num_long,
+                                                       m.num_heavy, m.heavy_sub, g.light,
+                                                       static_cast<const V*>(m.chunk_sum), static_cast<V*>(y), *epi);
     else
-      sliced_long_fixup<V><<<g, b, 0, s>>>(m.long_row, m.long_first, m.num_long, static_cast<const V*>(m.chunk_sum),
-                                           static_cast<V*>(y));
+      sliced_long_fixup<V><<<g.total, b, 0, s>>>(m.long_row, m.long_first, m.long_heavy, m.num_long, m.num_heavy,
+                                                 m.heavy_sub, g.light, static_cast<const V*>(m.chunk_sum),
+                                                 static_cast<V*>(y));
     if (!VNEC_CUDA(cudaGetLastError())) return false;
   }
   if (epi && !fused && !apply_epilogue(y, m.n_rows, sizeof(V) == 8, *epi, s)) return false;

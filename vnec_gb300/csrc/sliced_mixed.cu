@@ -28,6 +28,7 @@
 
 #include "common.h"
 #include "df32.cuh"
+#include "long_rows.cuh"
 #include "sliced.h"
 #include "vnec_gb300.h"
 
@@ -531,14 +532,12 @@ sliced_mixed_kernel(const SlicedTask* __restrict__ tasks, long long num_tasks, c
 }
 
 __global__ void long_fixup_f64(const int32_t* __restrict__ long_row, const int32_t* __restrict__ long_first,
-                               long long num_long, const double* __restrict__ chunk_sum, double* __restrict__ y,
-                               int* flag) {
-  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i == 0 && flag) *flag = 0;  // consumed: reset for the next call
-  if (i >= num_long) return;
-  double s = 0.0;
-  for (int c = long_first[i]; c < long_first[i + 1]; ++c) s += chunk_sum[c];
-  y[long_row[i]] = s;
+                               const int32_t* __restrict__ long_heavy, long long num_long, long long num_heavy,
+                               long long heavy_sub, unsigned light_blocks, const double* __restrict__ chunk_sum,
+                               double* __restrict__ y, int* flag) {
+  if (blockIdx.x == 0 && threadIdx.x == 0 && flag) *flag = 0;  // consumed: reset for the next call
+  long_rows_fixup<double>(long_first, long_heavy, num_long, num_heavy, heavy_sub, light_blocks, chunk_sum,
+                          [&](long long i, double s) { y[long_row[i]] = s; });
 }
 
 __global__ void reset_flag(int* flag) { *flag = 0; }
@@ -614,9 +613,10 @@ bool sliced_mixed_spmv(const SlicedMatrix& m, const SlicedMixed& mx, const doubl
   }
   if (m.num_long > 0) {
     const int b = 128;
-    long_fixup_f64<<<(unsigned)((m.num_long + b - 1) / b), b, 0, s>>>(
-        m.long_row, m.long_first, m.num_long, static_cast<const double*>(m.chunk_sum), y,
-        mx.precision == kPrecDF32 ? mx.flag : nullptr);
+    const FixupGrid g = fixup_grid(m, b);
+    long_fixup_f64<<<g.total, b, 0, s>>>(m.long_row, m.long_first, m.long_heavy, m.num_long, m.num_heavy,
+                                         m.heavy_sub, g.light, static_cast<const double*>(m.chunk_sum), y,
+                                         mx.precision == kPrecDF32 ? mx.flag : nullptr);
     if (!VNEC_CUDA(cudaGetLastError())) return false;
   } else if (mx.precision == kPrecDF32) {
     reset_flag<<<1, 1, 0, s>>>(mx.flag);

@@ -17,7 +17,7 @@ struct SlicedPlan final : Plan {
   SlicedMatrix m;
   SlicedMixed mx;  // precision form (FP64 = plain)
   DeviceBuffer tasks, val, col, rowid, long_row, long_first, chunk_sum, xbuf, flag, row_scale, chunk_scale;
-  DeviceBuffer hot_cols, xhot, col16, first, val_split, pat16;
+  DeviceBuffer hot_cols, xhot, col16, first, val_split, pat16, long_heavy;
   std::vector<int32_t> hot_host;  // hot-column window: original column of each slot
   SlicedParams prm;
   int64_t blocks = 0;  // dense-block plans: number of blocks of 4
@@ -27,6 +27,7 @@ struct SlicedPlan final : Plan {
   // the copy of one part's y rows to the host overlaps the next part's SpMV.
   struct Part {
     int64_t t0, t1, l0, l1, r0, r1;  // task, long-row and row ranges
+    int64_t h0, h1;                  // heavy long rows (SlicedMatrix::long_heavy) of the part
   };
   std::vector<Part> parts;
   // Each part runs on its own stream, with stream priorities falling from the
@@ -123,6 +124,9 @@ struct SlicedPlan final : Plan {
       mp.long_row = m.long_row + q.l0;
       mp.long_first = m.long_first + q.l0;
       mp.num_long = q.l1 - q.l0;
+      mp.long_heavy = m.long_heavy + q.h0;
+      mp.num_heavy = q.h1 - q.h0;
+      mp.heavy_sub = q.l0;
       mp.hot_ready = true;  // gathered above
       if (!sliced_spmv(mp, type == SpB_FP64, dx.ptr, dy.ptr, cs) || !VNEC_CUDA(cudaEventRecord(part_done[i], cs)) ||
           !VNEC_CUDA(cudaStreamWaitEvent(copy_stream, part_done[i], 0)))
@@ -414,6 +418,10 @@ std::unique_ptr<Plan> upload(std::unique_ptr<SlicedPlan> p, SlicedHost* h, int v
       col16 = col16_runs.data();
     }
   }
+  // Long rows whose chunk sums one warp adds up in the fix-up launch.
+  std::vector<int32_t> heavy;
+  for (int64_t i = 0; i < hv.num_long; ++i)
+    if (hv.long_first[i + 1] - hv.long_first[i] > kHeavyChunks) heavy.push_back((int32_t)i);
   auto up = [](DeviceBuffer& b, const void* src, size_t bytes, size_t alloc) {
     if (!b.alloc(std::max(alloc, bytes))) return false;
     return bytes == 0 || VNEC_CUDA(cudaMemcpy(b.ptr, src, bytes, cudaMemcpyHostToDevice));
@@ -424,6 +432,7 @@ std::unique_ptr<Plan> upload(std::unique_ptr<SlicedPlan> p, SlicedHost* h, int v
       !up(p->rowid, hv.rowid, 4 * (size_t)hv.n_rowid, 4 * (size_t)hv.n_rowid + 64) ||
       !up(p->long_row, hv.long_row, 4 * (size_t)hv.num_long, 4 * (size_t)hv.num_long + 64) ||
       !up(p->long_first, hv.long_first, 4 * (size_t)(hv.num_long + 1), 0) ||
+      !up(p->long_heavy, heavy.data(), 4 * heavy.size(), 4 * heavy.size() + 64) ||
       !p->chunk_sum.alloc((size_t)vb * (hv.num_chunks + 1)))
     return nullptr;
   const int64_t nhot = (int64_t)p->hot_host.size();
@@ -488,6 +497,8 @@ std::unique_ptr<Plan> upload(std::unique_ptr<SlicedPlan> p, SlicedHost* h, int v
   m.rowid = p->rowid.as<int32_t>();
   m.long_row = p->long_row.as<int32_t>();
   m.long_first = p->long_first.as<int32_t>();
+  m.long_heavy = p->long_heavy.as<int32_t>();
+  m.num_heavy = (int64_t)heavy.size();
   m.chunk_sum = p->chunk_sum.ptr;
   m.lane_run = run;
   p->delta_nnz = hv.col16 ? hv.delta_nnz : 0;
@@ -514,8 +525,11 @@ std::unique_ptr<Plan> upload(std::unique_ptr<SlicedPlan> p, SlicedHost* h, int v
       int64_t w1 = w0 + 1;
       while (w1 < hv.num_windows && hv.win_entry[w1] < target) ++w1;
       if (i == kParts) w1 = hv.num_windows;
-      p->parts.push_back(SlicedPlan::Part{hv.win_task[w0], hv.win_task[w1], hv.win_long[w0], hv.win_long[w1],
-                                          w0 * W, std::min<int64_t>(p->n_rows, w1 * W)});
+      const int64_t l0 = hv.win_long[w0], l1 = hv.win_long[w1];
+      const int64_t h0 = std::lower_bound(heavy.begin(), heavy.end(), (int32_t)l0) - heavy.begin();
+      const int64_t h1 = std::lower_bound(heavy.begin(), heavy.end(), (int32_t)l1) - heavy.begin();
+      p->parts.push_back(SlicedPlan::Part{hv.win_task[w0], hv.win_task[w1], l0, l1,
+                                          w0 * W, std::min<int64_t>(p->n_rows, w1 * W), h0, h1});
       w0 = w1;
     }
   }
