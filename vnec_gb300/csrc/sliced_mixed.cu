@@ -39,8 +39,9 @@ constexpr unsigned kFull = 0xffffffffu;
 constexpr int kWarps = 8;
 
 // Round-to-nearest-even FP64 -> FP32 from the bit patterns (IEEE 754:
-// overflow to infinity, gradual underflow to subnormals, NaN stays NaN).
-__device__ __forceinline__ float f64_to_f32_rne(double v) {
+// overflow to infinity, gradual underflow to subnormals, NaN stays NaN):
+// every case, in 64-bit integer arithmetic.
+__device__ __noinline__ float f64_to_f32_rne_general(double v) {
   const unsigned long long b = static_cast<unsigned long long>(__double_as_longlong(v));
   const unsigned sign = static_cast<unsigned>(b >> 63) << 31;
   const int e = static_cast<int>((b >> 52) & 0x7ff);
@@ -76,6 +77,25 @@ __device__ __forceinline__ float f64_to_f32_rne(double v) {
     bits = (expo << 23) | (static_cast<unsigned>(q) & 0x7FFFFFu);
   }
   return __uint_as_float(sign | bits);
+}
+
+// The same rounding with a 32-bit fast path for the usual case, an FP64
+// exponent inside FP32's normal range (2^-126 <= |v| < 2^128): the high word
+// rebiased and shifted gives the sign, exponent and top 20 fraction bits,
+// the low word's top 3 bits complete the 23, and adding the round bit (bit
+// 28 of the low word) when the bits below it are not all zero or the kept
+// lsb is odd rounds to nearest even; a carry out of the fraction moves to
+// the next binade, and out of exponent 254 to infinity, as IEEE 754 wants.
+__device__ __forceinline__ float f64_to_f32_rne(double v) {
+  const unsigned long long b = static_cast<unsigned long long>(__double_as_longlong(v));
+  const unsigned hi = static_cast<unsigned>(b >> 32), lo = static_cast<unsigned>(b);
+  const unsigned e = (hi >> 20) & 0x7ffu;
+  if (e - 897u < 254u) {
+    const unsigned bits = (hi & 0x80000000u) | (((hi & 0x7fffffffu) - (896u << 20)) << 3) | (lo >> 29);
+    const unsigned up = (lo >> 28) & (((lo & 0x0fffffffu) != 0u) | (lo >> 29)) & 1u;
+    return __uint_as_float(bits + up);
+  }
+  return f64_to_f32_rne_general(v);
 }
 
 }  // namespace
