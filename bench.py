@@ -701,7 +701,7 @@ def batch_legs(mats, ks, precs, steps: int, warmup: int, dev, flush, stream, ws:
             if tile:  # fixed layout (lanes, long-row limit, warps per block, unroll), no autotune
                 plan = api.BatchPlan(mats, k, precision=prec, lanes=tile[0], long_row_len=tile[1],
                                      warps_per_block=tile[2], unroll=tile[3],
-                                     dispatch=tile[4] if len(tile) > 4 else 0)
+                                     dispatch=tile[4] if len(tile) > 4 else 0, k1_layout=-1)
             else:
                 plan = api.BatchPlan(mats, k, precision=prec, autotune=True)
             t_plan = time.time() - t_plan
@@ -765,7 +765,10 @@ def batch_legs(mats, ks, precs, steps: int, warmup: int, dev, flush, stream, ws:
                    "e2e_gbs": round(B * pipe_steps / pipe_s / 1e9, 2),
                    "e2e_sync_gbs": round(B * e2e_steps / e2e_s / 1e9, 2),
                    "h2d_bytes_per_step": n_cols * k * 8, "d2h_bytes_per_step": n_rows * k * 8,
-                   "algorithmic_bytes": B, "lanes": info.lanes, "long_row_len": info.long_row_len,
+                   "algorithmic_bytes": B,
+                   "layout": ("one sliced row-group plan of the block-diagonal concatenation (k = 1), unroll "
+                              f"{info.items_per_thread}" if info.lanes == 0 else "batch kernel"),
+                   "lanes": info.lanes, "long_row_len": info.long_row_len,
                    "threads_per_block": info.threads_per_block, "tasks": info.num_tiles,
                    "tuner": {"candidates": len(cand), "best_ms_on_sample": round(tms[best], 4) if cand else None,
                              "worst_ms_on_sample": round(max(tms), 4) if cand else None,

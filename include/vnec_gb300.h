@@ -281,7 +281,9 @@ typedef struct {
   int64_t blocks;          /* dense-block plans: blocks of 4 columns (fill = nnz / (4 * blocks)) */
   int precision;           /* SpB_VNEC_precision_ext of a sliced or batch plan */
   int rhs;                 /* right-hand sides k (1 for single-vector plans) */
-  int lanes;               /* batch plans: lanes per row (items_per_thread = k / lanes per lane) */
+  int lanes;               /* batch plans: lanes per row (items_per_thread = k / lanes per lane);
+                              0 for a k = 1 batch run as one sliced plan (items_per_thread is then
+                              its unroll) */
   int long_row_len;        /* sliced and batch plans: rows longer than this are chunked */
 } SpB_VNEC_info_ext;
 
@@ -458,7 +460,14 @@ typedef struct {
                           compute (0: 8, 1: one part) */
   int dispatch;        /* 0: default, 1: persistent warps striding the task list, 2: one warp per task
                           (blocks dispatched in task order, so the tasks in flight stay a compact window) */
-  int reserved[4];
+  int k1_layout;       /* k = 1 only.  0 (default): the batch runs as one sliced row-group plan (the
+                          SpB_VNEC_KERNEL_S layout, unroll timed at build) of the block-diagonal
+                          concatenation, in the same precision form: at one right-hand side the batch
+                          is one sparse matrix, and that layout's 16-bit deltas, hot-column window and
+                          long-row fix-up serve it best (512 uneven matrices: FP64 2.15 -> 1.83 ms);
+                          lanes, long_row_len, chunk, warps_per_block, unroll and dispatch do not apply,
+                          and the plan reports lanes = 0.  -1: the batch kernel. */
+  int reserved[3];
 } SpB_VNEC_batch_options_ext;
 
 /* Plan from host CSR arrays per matrix: int64 row offsets (n_rows[m] + 1),

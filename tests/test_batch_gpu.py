@@ -94,7 +94,8 @@ def test_batch_all_lanes(built, batch, k, precision):
     from vnec_gb300 import api
 
     for L, unroll in [(L, u) for L in lanes_for(k) for u in (1, 2, 3)]:
-        p = api.BatchPlan(batch, k, lanes=L, long_row_len=64, precision=precision, max_steps=4, unroll=unroll)
+        p = api.BatchPlan(batch, k, lanes=L, long_row_len=64, precision=precision, max_steps=4, unroll=unroll,
+                          k1_layout=-1)
         try:
             ro, co = p.offsets()
             X = _x(p, k)
@@ -120,7 +121,8 @@ def test_batch_staged_entries_bit_identical(built, batch, k, precision):
     for L in lanes_for(k):
         ys = []
         for unroll in (1, 3):
-            p = api.BatchPlan(batch, k, lanes=L, long_row_len=2048, precision=precision, unroll=unroll)
+            p = api.BatchPlan(batch, k, lanes=L, long_row_len=2048, precision=precision, unroll=unroll,
+                              k1_layout=-1)
             try:
                 ys.append(p.mxv_host(_x(p, k)))
             finally:
@@ -323,7 +325,7 @@ def test_batch_dispatch_modes_bit_identical(built, batch, k, precision):
 
     outs = []
     for dispatch in (1, 2):
-        p = api.BatchPlan(batch, k, precision=precision, long_row_len=64, dispatch=dispatch)
+        p = api.BatchPlan(batch, k, precision=precision, long_row_len=64, dispatch=dispatch, k1_layout=-1)
         try:
             X = _x(p, k)
             outs.append(p.mxv_host(X))
@@ -339,3 +341,67 @@ def test_batch_dispatch_modes_bit_identical(built, batch, k, precision):
         check(p.mxv_host(X), Yref, cond, TOL[precision])
     finally:
         p.free()
+
+
+@pytest.mark.parametrize("precision", [0, 1, 3], ids=["fp64", "fp32", "df32"])
+def test_batch_k1_runs_as_one_sliced_plan(built, batch, precision):
+    """At k = 1 the batch runs as one sliced plan of its block-diagonal
+    concatenation (the default, reported as lanes = 0).  It and the batch
+    kernel (k1_layout = -1) both meet the form's tolerance against the oracle;
+    the device call with and without a graph, the host call in parts and
+    pipelined host calls give the same bits; the DF32 guard covers
+    out-of-range X."""
+    import torch
+
+    from vnec_gb300 import api
+
+    ref = api.BatchPlan(batch, 1, precision=precision, k1_layout=-1)
+    try:
+        ro, co = ref.offsets()
+        X = _x(ref, 1, seed=5)
+        Yref, cond = oracle_batch(batch, X, 1, co, ro)
+        Yk = ref.mxv_host(X)
+        assert ref.info().lanes >= 1
+    finally:
+        ref.free()
+    check(Yk, Yref, cond, TOL[precision])
+    outs = []
+    for graph in (True, False):
+        p = api.BatchPlan(batch, 1, precision=precision, graph=graph, host_parts=3, window_rows=500)
+        try:
+            inf = p.info()
+            assert inf.kernel == api.KERNEL_BATCH and inf.lanes == 0 and inf.rhs == 1
+            assert inf.items_per_thread in (4, 8, 12, 16) and inf.precision == precision
+            assert np.array_equal(p.offsets()[0], ro) and np.array_equal(p.offsets()[1], co)
+            Y = p.mxv_host(X)
+            check(Y, Yref, cond, TOL[precision])
+            x = torch.from_numpy(X).cuda()
+            y = torch.full((int(ro[-1]),), float("nan"), dtype=torch.float64, device="cuda")
+            for _ in range(2):
+                p.mxv_device(x.data_ptr(), y.data_ptr())
+            torch.cuda.synchronize()
+            assert y.cpu().numpy().tobytes() == Y.reshape(-1).tobytes()
+            hx = torch.from_numpy(X).pin_memory()
+            hys = [torch.empty(int(ro[-1]), dtype=torch.float64).pin_memory() for _ in range(3)]
+            for hy in hys:
+                p.mxv_host_async(hx.numpy(), hy.numpy())
+            p.host_wait()
+            for hy in hys:
+                assert hy.numpy().tobytes() == Y.reshape(-1).tobytes()
+            if precision == api.PREC_DF32:
+                Xb = X.copy()
+                Xb[::13] = 1e30
+                Yb, condb = oracle_batch(batch, Xb, 1, co, ro)
+                check(p.mxv_host(Xb), Yb, condb, TOL[precision])
+            outs.append(Y)
+        finally:
+            p.free()
+    assert outs[0].tobytes() == outs[1].tobytes()
+
+
+def test_batch_k1_layout_option_checked(built, batch):
+    from vnec_gb300 import api
+
+    for bad in (1, -2):
+        with pytest.raises(api.VnecError, match="k1_layout"):
+            api.BatchPlan(batch, 1, k1_layout=bad)

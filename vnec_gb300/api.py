@@ -87,7 +87,7 @@ class BatchOptions(C.Structure):
     _fields_ = [("precision", C.c_int), ("lanes", C.c_int), ("long_row_len", C.c_int), ("chunk", C.c_int),
                 ("warps_per_block", C.c_int), ("autotune", C.c_int), ("no_graph", C.c_int),
                 ("window_rows", C.c_int), ("max_steps", C.c_int), ("unroll", C.c_int), ("host_parts", C.c_int),
-                ("dispatch", C.c_int), ("reserved", C.c_int * 4)]
+                ("dispatch", C.c_int), ("k1_layout", C.c_int), ("reserved", C.c_int * 3)]
 
 
 _vp = C.c_void_p
@@ -516,9 +516,10 @@ class Plan:
 def batch_options(precision: int = PREC_FP64, lanes: int = 0, long_row_len: int = 0, chunk: int = 0,
                   warps_per_block: int = 0, autotune: bool = False, graph: bool = True,
                   window_rows: int = 0, max_steps: int = 0, unroll: int = 0, host_parts: int = 0,
-                  dispatch: int = 0) -> BatchOptions:
+                  dispatch: int = 0, k1_layout: int = 0) -> BatchOptions:
     o = BatchOptions()
     o.max_steps, o.unroll, o.host_parts, o.dispatch = max_steps, unroll, host_parts, dispatch
+    o.k1_layout = k1_layout
     o.precision, o.lanes, o.long_row_len, o.chunk = precision, lanes, long_row_len, chunk
     o.warps_per_block, o.autotune, o.no_graph, o.window_rows = warps_per_block, int(autotune), int(not graph), \
         window_rows

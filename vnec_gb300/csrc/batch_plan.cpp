@@ -6,11 +6,13 @@
 #include <omp.h>
 
 #include <algorithm>
+#include <climits>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <map>
+#include <memory>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -408,6 +410,9 @@ bool whole_batch_dispatch(BatchMatrix& m, int64_t n_rows, int64_t n_cols, int k,
 // ---------------------------------------------------------------------------
 
 struct BatchPlan final : Plan {
+  // k = 1 batches (SpB_VNEC_batch_options_ext::k1_layout 0): one sliced plan
+  // of the block-diagonal concatenation runs every call; `d` stays empty.
+  std::unique_ptr<Plan> k1;
   BatchDev d;
   BatchParams prm;
   TuneRun tuning;
@@ -448,6 +453,12 @@ struct BatchPlan final : Plan {
   }
 
   bool run_host(const void* h_x, void* h_y) override {
+    if (k1) {
+      std::lock_guard<std::mutex> g(host_mu);
+      if (!drain_pipe()) return false;
+      k1->profiling = profiling;
+      return k1->run_host(h_x, h_y);
+    }
     if (parts.size() < 2 || profiling) return Plan::run_host(h_x, h_y);
     std::lock_guard<std::mutex> g(host_mu);
     if (!drain_pipe()) return false;
@@ -489,13 +500,30 @@ struct BatchPlan final : Plan {
   // Pipelined host calls alternate two buffer slots: direct launches (one or
   // two kernels) instead of re-pointing the graph on every call.
   bool run_slot(int, const void* d_x, void* d_y, cudaStream_t s) override {
+    if (k1) {
+      k1->profiling = false;
+      return k1->run(d_x, d_y, s);
+    }
     return batch_spmm(d.m, static_cast<const double*>(d_x), static_cast<double*>(d_y), s);
+  }
+  // One call's kernels on `s`: the sliced plan's for a k = 1 batch, else the batch kernel's.
+  bool enqueue(const void* d_x, void* d_y, cudaStream_t s) {
+    if (k1) {
+      k1->profiling = profiling;
+      return k1->run(d_x, d_y, s);
+    }
+    return batch_spmm(d.m, static_cast<const double*>(d_x), static_cast<double*>(d_y), s);
+  }
+  bool run_epilogue(const void* d_x, void* d_y, const SlicedEpilogue& e, cudaStream_t s) override {
+    if (!k1) return Plan::run_epilogue(d_x, d_y, e, s);
+    k1->profiling = profiling;
+    return k1->run_epilogue(d_x, d_y, e, s);
   }
 
   bool capture(const void* d_x, void* d_y) {
     if (!cap && !VNEC_CUDA(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking))) return false;
     if (!VNEC_CUDA(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal))) return false;
-    const bool ok = batch_spmm(d.m, static_cast<const double*>(d_x), static_cast<double*>(d_y), cap);
+    const bool ok = enqueue(d_x, d_y, cap);
     cudaGraph_t g = nullptr;
     const cudaError_t e = cudaStreamEndCapture(cap, &g);
     if (!ok || !VNEC_CUDA(e)) {
@@ -522,34 +550,48 @@ struct BatchPlan final : Plan {
   }
 
   bool run(const void* d_x, void* d_y, cudaStream_t s) override {
-    const int R = d.m.k / d.m.lanes;
+    const int R = k1 ? 1 : d.m.k / d.m.lanes;
     if (R >= 2 && ((reinterpret_cast<uintptr_t>(d_x) | reinterpret_cast<uintptr_t>(d_y)) & 15)) {
       set_error("batch: x and y must be 16-byte aligned for this plan's layout");
       return false;
     }
+    if (profiling && k1) return enqueue(d_x, d_y, s);
     if (profiling) {
       if (!ensure_events() || !VNEC_CUDA(cudaEventRecord(events[0], s))) return false;
       if (!batch_spmm(d.m, static_cast<const double*>(d_x), static_cast<double*>(d_y), s)) return false;
       return VNEC_CUDA(cudaEventRecord(events[1], s));
     }
-    if (!use_graph) return batch_spmm(d.m, static_cast<const double*>(d_x), static_cast<double*>(d_y), s);
+    if (!use_graph) return enqueue(d_x, d_y, s);
     std::lock_guard<std::mutex> g(gmu);
     if ((!exec || gx != d_x || gy != d_y) && !capture(d_x, d_y)) return false;
     return VNEC_CUDA(cudaGraphLaunch(exec, s));
   }
   int kernel_ms(float* ms, int cap_n) const override {
+    if (k1) return k1->kernel_ms(ms, cap_n);
     if (!profiling || !events[0] || cap_n < 1) return 0;
     if (cudaEventSynchronize(events[1]) != cudaSuccess) return 0;
     cudaEventElapsedTime(&ms[0], events[0], events[1]);
     return 1;
   }
-  int launches_per_call() const override { return n_rows == 0 && precision != kPrecFP32 ? 0 : batch_launches(d.m); }
-  int64_t device_bytes() const override { return d.bytes() + (int64_t)(dx.bytes + dy.bytes); }
+  int launches_per_call() const override {
+    if (k1) return k1->launches_per_call();
+    return n_rows == 0 && precision != kPrecFP32 ? 0 : batch_launches(d.m);
+  }
+  int64_t device_bytes() const override {
+    return (k1 ? k1->device_bytes() : d.bytes()) + (int64_t)(dx.bytes + dy.bytes);
+  }
   int64_t algorithmic_bytes() const override {
     const int64_t vb = precision == kPrecFP32 ? 4 : 8;  // DF32 stores (hi, lo) float pairs
     return nnz * (vb + 4) + (n_rows + (int64_t)row_off.size() - 1) * 4 + (n_cols + n_rows) * rhs * 8;
   }
   void describe(SpB_VNEC_info_ext* info) const override {
+    if (k1) {
+      k1->describe(info);
+      info->kernel = SpB_VNEC_KERNEL_BATCH;
+      info->rhs = rhs;
+      info->lanes = 0;
+      return;
+    }
     info->kernel = SpB_VNEC_KERNEL_BATCH;
     info->threads_per_block = d.m.warps_per_block * 32;
     info->items_per_thread = d.m.k / d.m.lanes;
@@ -591,6 +633,51 @@ void plan_parts(BatchPlan* p, const BatchHostView& hv, int n_parts) {
   }
 }
 
+// A k = 1 batch as one sliced plan: the block-diagonal concatenation (matrix
+// m's rows at row_off[m], its columns shifted by col_off[m]) in CSR, planned
+// with the batch's precision form and the sliced defaults.
+bool build_k1(BatchPlan* p, const BatchSource& s, const SpB_VNEC_batch_options_ext& o) {
+  const int n = s.size();
+  if (p->n_rows > INT32_MAX || p->n_cols > INT32_MAX) {
+    set_error("batch: more than 2^31 rows or columns");
+    return false;
+  }
+  std::vector<int64_t> z_off((size_t)n + 1, 0);
+  for (int m = 0; m < n; ++m) z_off[(size_t)m + 1] = z_off[(size_t)m] + s.rp[(size_t)m][s.n_rows[(size_t)m]];
+  std::vector<int64_t> rp((size_t)p->n_rows + 1, 0);
+  std::vector<int32_t> ci((size_t)z_off[(size_t)n]);
+  std::vector<double> val((size_t)z_off[(size_t)n]);
+#pragma omp parallel for schedule(dynamic, 1)
+  for (int m = 0; m < n; ++m) {
+    const int64_t r0 = p->row_off[(size_t)m], c0 = p->col_off[(size_t)m], z0 = z_off[(size_t)m];
+    const int64_t* src_rp = s.rp[(size_t)m];
+    const int64_t base = src_rp[0];
+    for (int64_t r = 0; r < s.n_rows[(size_t)m]; ++r) rp[(size_t)(r0 + r + 1)] = z0 + src_rp[r + 1] - base;
+    const int64_t nz = src_rp[s.n_rows[(size_t)m]] - base;
+    for (int64_t q = 0; q < nz; ++q) {
+      ci[(size_t)(z0 + q)] = (int32_t)(s.ci[(size_t)m][base + q] + c0);
+      val[(size_t)(z0 + q)] = s.val[(size_t)m][base + q];
+    }
+  }
+  CsrView v;
+  v.type = SpB_FP64;
+  v.n_rows = p->n_rows;
+  v.n_cols = p->n_cols;
+  v.nnz = z_off[(size_t)n];
+  v.ptr = rp.data();
+  v.idx = ci.data();
+  v.val = val.data();
+  SpB_VNEC_options_ext so;
+  std::memset(&so, 0, sizeof(so));
+  so.kernel = SpB_VNEC_KERNEL_S;
+  so.precision = o.precision;
+  so.window_rows = o.window_rows;
+  so.max_steps = o.max_steps;
+  so.host_parts = o.host_parts;
+  p->k1 = build_sliced(v, &so);
+  return p->k1 != nullptr;
+}
+
 }  // namespace
 
 std::unique_ptr<Plan> build_batch(int n, const CsrView* mats, int k, const SpB_VNEC_batch_options_ext* opts) {
@@ -620,6 +707,10 @@ std::unique_ptr<Plan> build_batch(int n, const CsrView* mats, int k, const SpB_V
   if (o.long_row_len < 0 || o.chunk < 0 || o.window_rows < 0 || o.max_steps < 0 || o.unroll < 0 || o.unroll > 3 ||
       o.dispatch < 0 || o.dispatch > 2) {
     set_error("batch: negative option");
+    return nullptr;
+  }
+  if (o.k1_layout != 0 && o.k1_layout != -1) {
+    set_error("batch: k1_layout must be 0 (sliced plan at k = 1) or -1 (batch kernel)");
     return nullptr;
   }
   auto p = std::make_unique<BatchPlan>();
@@ -663,6 +754,10 @@ std::unique_ptr<Plan> build_batch(int n, const CsrView* mats, int k, const SpB_V
   p->n_cols = p->col_off[(size_t)n];
   BatchSource src;
   make_source(n, mats, &src);
+  if (k == 1 && o.k1_layout == 0) {
+    if (!build_k1(p.get(), src, o)) return nullptr;
+    return p;
+  }
 
   TuneChoice choice;
   choice.lanes = o.lanes > 0 ? o.lanes : std::min(k, 32);
