@@ -435,8 +435,10 @@ int SpB_VNEC_builtin_model_ext(float *params, float *feature_range);
  * concatenations of the X_m and Y_m in matrix order (offsets from
  * SpB_VNEC_batch_offsets_ext, in rows of k values), so one
  * SpB_mxv_device_ext / SpB_mxv_host_ext call runs the whole batch: one
- * persistent kernel (the FP32 form adds one launch that rounds X), replayed
- * from a CUDA graph captured on the first call with a given (x, y) pair.
+ * persistent kernel (the FP32 form adds one launch that rounds X), or for
+ * k = 1 the kernels of one sliced plan of the concatenation (k1_layout),
+ * replayed from a CUDA graph captured on the first call with a given (x, y)
+ * pair.
  * Device x and y must be 16-byte aligned when k / lanes >= 2.  Calls on one
  * batch plan must not overlap on the GPU (they share the plan's long-row
  * scratch). */
