@@ -189,7 +189,14 @@ typedef struct {
   int shared_patterns;   /* sliced precision forms: groups of rows with equal length and the
                             same column gaps (stencils, banded rows) read one copy of the gaps
                             per group (0: on, -1: off; the sums are the same either way) */
-  int reserved[5];
+  int l2_prefetch;       /* sliced plans: each warp has the L2 prefetch the stored entries (values
+                            and columns) this many entries past its own task's, and the task
+                            metadata the same distance ahead, so that the tasks' loads meet
+                            L2 instead of HBM (0: 262,144 where most nonzeros sit in 16-bit-delta
+                            row groups, i.e. local columns, off for gather-bound layouts; -1:
+                            off; > 0: the distance, rounded down to a multiple of 32; the sums
+                            are the same either way) */
+  int reserved[4];
 } SpB_VNEC_options_ext;
 
 /* Precision forms of the sliced kernel for an FP64 matrix (x and y stay

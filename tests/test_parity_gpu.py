@@ -899,3 +899,29 @@ def test_f64_to_f32_rounding_matches_hardware(built):
     got1 = out1.cpu().numpy()
     assert np.array_equal(np.isnan(got1), nan[1:])
     assert np.array_equal(got1[~nan[1:]].view(np.uint32), ref[1:][~nan[1:]].view(np.uint32))
+
+
+@pytest.mark.parametrize("prec", [0, 1, 2, 3], ids=["fp64", "fp32", "bf16_rowscale", "df32"])
+def test_sliced_l2_prefetch_bit_identical(built, prec):
+    """The L2 prefetch ahead of the running tasks (the default on local
+    layouts, off on gather-bound ones) only moves data into L2 early: y is
+    bit-identical with it off, at the default and at explicit distances,
+    including host-vector calls split into parts (whose task indices count
+    from each part's first task), a distance beyond the matrix and row groups
+    cut into chunks."""
+    from vnec_gb300 import api
+    from vnec_gb300 import generators as G
+
+    mats = (G.stencil27(40, seed=3), G.banded(200000, 13, seed=2), G.rmat(15, 16 << 15, seed=4),
+            _edge_matrix("hub_rows_and_empties"))
+    for m in mats:
+        xv = G.vector(m.n_cols, seed=8)
+        ys = []
+        for lp in (-1, 0, 32, 4096, 1 << 20, 1 << 30):
+            p = api.Plan(m, kernel=api.KERNEL_S, precision=prec, l2_prefetch=lp, window_rows=1000,
+                         long_row_len=256)
+            ys.append(p.mxv_host(xv))
+            p.free()
+        for y in ys[1:]:
+            assert y.tobytes() == ys[0].tobytes()
+        check_f64(ys[0], m, xv, tol=PREC_TOL.get(prec, TOL_F64))

@@ -67,7 +67,7 @@ class Options(C.Structure):
                 ("precision", C.c_int), ("hot_columns", C.c_int), ("dense_fill_permille", C.c_int),
                 ("transpose", C.c_int), ("host_parts", C.c_int), ("column_deltas", C.c_int),
                 ("lane_vectors", C.c_int), ("hot_order", C.c_int), ("offsets64", C.c_int),
-                ("shared_patterns", C.c_int), ("reserved", C.c_int * 5)]
+                ("shared_patterns", C.c_int), ("l2_prefetch", C.c_int), ("reserved", C.c_int * 4)]
 
 
 class Info(C.Structure):
@@ -370,7 +370,7 @@ def options(kernel: int = KERNEL_AUTO, threads_per_block: int = 0, items_per_thr
             max_steps: int = 0, cache_hints: int = 0, precision: int = PREC_FP64, hot_columns: int = 0,
             dense_fill_permille: int = 0, transpose: bool = False, host_parts: int = 0,
             column_deltas: int = 0, lane_vectors: int = 0, hot_order: int = 0, offsets64: int = 0,
-            shared_patterns: int = 0) -> Options:
+            shared_patterns: int = 0, l2_prefetch: int = 0) -> Options:
     o = Options()
     o.kernel, o.threads_per_block, o.items_per_thread = kernel, threads_per_block, items_per_thread
     o.pipeline_stages, o.arithmetic = pipeline_stages, arithmetic
@@ -384,6 +384,7 @@ def options(kernel: int = KERNEL_AUTO, threads_per_block: int = 0, items_per_thr
     o.hot_order = hot_order
     o.offsets64 = offsets64
     o.shared_patterns = shared_patterns
+    o.l2_prefetch = l2_prefetch
     return o
 
 

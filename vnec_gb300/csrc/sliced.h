@@ -42,6 +42,15 @@ struct FixupGrid {
   unsigned light, total;
 };
 
+// L2 prefetch distance of a plan (prefetch.cuh): a warp prefetches the entries
+// `entries` past its task's, and the task descriptor, row slots and shared
+// pattern the same distance ahead, expressed in tasks and row slots.
+struct SlicedPrefetch {
+  long long entries = 0;  // 0: off
+  long long tasks = 0, rows = 0;
+  long long n_entries = 0, n_tasks = 0, n_rows = 0;  // array bounds
+};
+
 struct SlicedMatrix {
   int64_t n_rows = 0, n_cols = 0, nnz = 0, entries = 0;  // entries include padding
   int64_t num_tasks = 0, num_long = 0, num_chunks = 0;
@@ -70,6 +79,7 @@ struct SlicedMatrix {
   const uint16_t* col16 = nullptr;    // delta tasks (kSlicedDelta): 16-bit column deltas
   const int32_t* first = nullptr;     // delta tasks: first column of each row slot
   const uint16_t* pat16 = nullptr;    // shared-pattern tasks (kSlicedShared): one delta per step
+  SlicedPrefetch pf;                  // L2 prefetch ahead of the running tasks (prefetch.cuh), off by default
   // FP32 / BF16 forms: 0, or P when val / col / col16 hold each lane's entries
   // in runs of P consecutive steps.  Steps [P*b, P*b + P) of a task's lane l
   // sit at base + b*32*P + l*P + (step - P*b), so a lane reads a run with one

@@ -18,6 +18,7 @@
 
 #include "common.h"
 #include "long_rows.cuh"
+#include "prefetch.cuh"
 #include "sliced.h"
 
 namespace vnec {
@@ -204,10 +205,23 @@ __device__ __forceinline__ void sliced_task(long long w, int lane, const SlicedT
                                             const int32_t* __restrict__ rowid, const V* __restrict__ x, V* y,
                                             V* __restrict__ chunk_sum, const V* __restrict__ xh, int ncols,
                                             const SlicedEpilogue& ep, const uint16_t* __restrict__ col16,
-                                            const int32_t* __restrict__ first) {
+                                            const int32_t* __restrict__ first,
+                                            const SlicedPrefetch& pf = SlicedPrefetch()) {
   const int4 raw = __ldg(reinterpret_cast<const int4*>(tasks) + w);
   const int base = raw.x, row_base = raw.y, steps = raw.z, meta = raw.w;
   const int kind = meta & 15, vwl = (meta >> 4) & 15, nrows = (meta >> 8) & 0xff;
+  // The entries and task metadata ahead of this task, into L2 (prefetch.cuh).
+  if (pf.entries > 0) {
+    prefetch_l2_task_meta(pf, w, base, row_base, kind != kSlicedChunk, tasks, first, rowid, nullptr, lane);
+    const long long e0 = base + pf.entries, len = 32LL * steps;
+    if (kind != kSlicedZero && e0 + len <= pf.n_entries) {
+      prefetch_l2_range(val + e0, len, lane);
+      if (meta & kSlicedDelta)
+        prefetch_l2_range(col16 + e0, len, lane);
+      else
+        prefetch_l2_range(col + e0, len, lane);
+    }
+  }
   if (kind == kSlicedZero) {
     if (lane < nrows) {
       const int row = rowid[row_base + lane];
@@ -290,11 +304,11 @@ sliced_kernel(const SlicedTask* __restrict__ tasks, long long num_tasks, const V
               const int32_t* __restrict__ col, const int32_t* __restrict__ rowid, const V* __restrict__ x,
               V* y, V* __restrict__ chunk_sum, const V* __restrict__ xh = nullptr, int ncols = 0,
               SlicedEpilogue ep = SlicedEpilogue(), const uint16_t* __restrict__ col16 = nullptr,
-              const int32_t* __restrict__ first = nullptr) {
+              const int32_t* __restrict__ first = nullptr, SlicedPrefetch pf = SlicedPrefetch()) {
   const long long w = ((long long)blockIdx.x * kWarpsPerBlock) + (threadIdx.x >> 5);
   if (w >= num_tasks) return;
   sliced_task<V, U, H, HOT, EPI>(w, threadIdx.x & 31, tasks, val, col, rowid, x, y, chunk_sum, xh, ncols, ep, col16,
-                                 first);
+                                 first, pf);
 }
 
 // FP64 recompute of a DF32 call whose x left the split range: a small grid of
@@ -380,7 +394,7 @@ bool launch_main(const SlicedMatrix& m, const void* x, void* y, cudaStream_t s,
                                                       m.rowid, static_cast<const V*>(x), static_cast<V*>(y),
                                                       static_cast<V*>(m.chunk_sum),
                                                       static_cast<const V*>(m.xhot), (int)m.n_cols, ep, m.col16,
-                                                      m.first);
+                                                      m.first, m.pf);
   return VNEC_CUDA(cudaGetLastError());
 }
 

@@ -29,6 +29,7 @@
 #include "common.h"
 #include "df32.cuh"
 #include "long_rows.cuh"
+#include "prefetch.cuh"
 #include "sliced.h"
 #include "vnec_gb300.h"
 
@@ -248,7 +249,7 @@ sliced_mixed_kernel(const SlicedTask* __restrict__ tasks, long long num_tasks, c
                     double* __restrict__ y, double* __restrict__ chunk_sum, const signed char* __restrict__ row_scale,
                     const signed char* __restrict__ chunk_scale, const int* __restrict__ flag,
                     const uint16_t* __restrict__ col16, const int32_t* __restrict__ first,
-                    const uint16_t* __restrict__ pat16) {
+                    const uint16_t* __restrict__ pat16, SlicedPrefetch pf) {
   if (flag && *reinterpret_cast<const volatile int*>(flag)) return;  // DF32: x out of range, guard launch computes
   const long long w = ((long long)blockIdx.x * kWarps) + (threadIdx.x >> 5);
   const int lane = threadIdx.x & 31;
@@ -256,6 +257,16 @@ sliced_mixed_kernel(const SlicedTask* __restrict__ tasks, long long num_tasks, c
   const int4 raw = __ldg(reinterpret_cast<const int4*>(tasks) + w);
   const int base = raw.x, row_base = raw.y, steps = raw.z, meta = raw.w;
   const int kind = meta & 15, vwl = (meta >> 4) & 15, nrows = (meta >> 8) & 0xff;
+  // The values (and per-lane column deltas) `pf` entries past this task's,
+  // into L2 (prefetch.cuh).
+  if (pf.entries > 0) {
+    prefetch_l2_task_meta(pf, w, base, row_base, kind != kSlicedChunk, tasks, first, rowid, pat16, lane);
+    const long long e0 = base + pf.entries, len = 32LL * steps;
+    if (kind != kSlicedZero && e0 + len <= pf.n_entries) {
+      prefetch_l2_range(val + e0, len, lane);
+      if ((meta & kSlicedDelta) && !(SH && (meta & kSlicedShared))) prefetch_l2_range(col16 + e0, len, lane);
+    }
+  }
   if (kind == kSlicedZero) {
     if (lane < nrows) y[rowid[row_base + lane]] = 0.0;
     return;
@@ -594,7 +605,7 @@ bool launch_mixed(const SlicedMatrix& m, const SlicedMixed& mx, const void* xs, 
   const void* vals = std::is_same<typename C::Val, float2>::value ? static_cast<const void*>(mx.val_split) : m.val;
   kern<<<(unsigned)grid, kWarps * 32, 0, s>>>(m.tasks, m.num_tasks, static_cast<const typename C::Val*>(vals), m.col,
                                               m.rowid, xs, y, static_cast<double*>(m.chunk_sum), mx.row_scale,
-                                              mx.chunk_scale, flag, m.col16, m.first, m.pat16);
+                                              mx.chunk_scale, flag, m.col16, m.first, m.pat16, m.pf);
   return VNEC_CUDA(cudaGetLastError());
 }
 
