@@ -643,7 +643,8 @@ bool build_k1(BatchPlan* p, const BatchSource& s, const SpB_VNEC_batch_options_e
     return false;
   }
   std::vector<int64_t> z_off((size_t)n + 1, 0);
-  for (int m = 0; m < n; ++m) z_off[(size_t)m + 1] = z_off[(size_t)m] + s.rp[(size_t)m][s.n_rows[(size_t)m]];
+  for (int m = 0; m < n; ++m)
+    z_off[(size_t)m + 1] = z_off[(size_t)m] + s.rp[(size_t)m][s.n_rows[(size_t)m]] - s.rp[(size_t)m][0];
   std::vector<int64_t> rp((size_t)p->n_rows + 1, 0);
   std::vector<int32_t> ci((size_t)z_off[(size_t)n]);
   std::vector<double> val((size_t)z_off[(size_t)n]);

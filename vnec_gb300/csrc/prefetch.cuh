@@ -5,9 +5,10 @@
 // other warps the whole stream that distance ahead of the tasks running now.
 // The lanes issue one `prefetch.global.L2` per 128-byte line: no registers
 // stay busy waiting, and the values reach L2 before their task starts.  On
-// stream-bound layouts (the 27-point stencil's precision forms) this takes
-// the latency of HBM off the warps' chains; on gather-bound ones it only adds
-// requests, so plans enable it by layout.
+// stream-bound layouts (local columns: stencils, bands; every form, FP64
+// included) this takes the latency of HBM off the warps' chains; on
+// gather-bound ones (power-law columns) it only adds requests to the L2's
+// limiting request rate, so plans enable it by layout.
 #pragma once
 
 #include <cstdint>
